@@ -1,0 +1,110 @@
+/*
+ * Extensions of the GB300 matchgate library beyond the reference's C API.
+ * Nothing here changes the meaning of a reference entry point; these add
+ * precision control, GPU-resident target maps, device-resident evaluation plans
+ * for callers that keep their data on the GPU, and results the reference only
+ * computes inside larger calls.
+ */
+#pragma once
+
+#include "matchgate_target.h"
+#include "trust_region.h"
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---------------------------------------------------------------------------------
+ * Precision of the batched evaluations (matchgate_target.h entry points).
+ *   MG_PREC_FP64  complex128 sweeps and sums (default; matches the reference)
+ *   MG_PREC_MIXED float-float sweeps (pairs of FP32, about 48 significant bits),
+ *                 compensated FP32 products and sums, FP64 final reductions
+ *   MG_PREC_FP32  complex FP32 sweeps, compensated FP32 sums into FP64
+ * Projection, retraction and the trust-region subproblem always run in FP64.
+ * --------------------------------------------------------------------------------- */
+enum { MG_PREC_FP64 = 0, MG_PREC_MIXED = 1, MG_PREC_FP32 = 2 };
+int mg_set_precision(int precision);
+int mg_get_precision(void);
+
+/* Tuning options (0 = automatic).  TILE_BITS: log2 of amplitudes per shared-memory
+ * tile; THREADS: threads per block; CHUNK_COLUMNS: basis columns per batch when
+ * columns are materialised from a host map or a Hessian is requested;
+ * CTAS_PER_SM: resident blocks per SM for the persistent grid. */
+enum { MG_OPT_TILE_BITS = 1, MG_OPT_THREADS = 2, MG_OPT_CHUNK_COLUMNS = 3, MG_OPT_CTAS_PER_SM = 4 };
+int mg_set_option(int option, long value);
+long mg_get_option(int option);
+
+/* Last error message of this thread's most recent failing call ("" if none). */
+const char* mg_last_error(void);
+
+/* ---------------------------------------------------------------------------------
+ * GPU-resident target maps.  Each constructor returns the `udata` to pass together
+ * with `mg_target_apply` as the (ufunc, udata) pair of any matchgate_target.h call;
+ * the library recognises the pair and applies U on the GPU per basis column instead
+ * of calling a host function 2^L times.  mg_target_apply itself applies U to a host
+ * vector (on the GPU), so the pair also works wherever a linear_func is called.
+ * --------------------------------------------------------------------------------- */
+int mg_target_apply(const struct statevector* restrict psi, void* udata, struct statevector* restrict psi_out);
+void* mg_target_brickwall(const struct matchgate ulist[], int ulayers, const int* uperms[], int nqubits);
+void* mg_target_circuit(const struct matchgate gates[], int ngates, const int wires[], int nqubits);
+void* mg_target_dense(const numeric* U, int nqubits);   /* row-major 2^L x 2^L */
+void mg_target_free(void* udata);
+/* Keep the conjugated target columns -conj(U e_b) resident in GPU memory after their
+ * first use (about 2^(2L-1) amplitudes), so later evaluations against the same target
+ * skip re-applying U.  Off by default. */
+int mg_target_set_resident(void* udata, int enable);
+
+/* ---------------------------------------------------------------------------------
+ * Results the reference computes only inside larger calls
+ * --------------------------------------------------------------------------------- */
+
+/* f and the Riemannian gradient vector grad_vec[8*nlayers] (the conjugated,
+ * tangent-projected layer gradients of src/matchgate_target.c:903-908) without a
+ * Hessian; the reference names this entry point in src/mg_brickwall_opt.c:47. */
+int matchgate_brickwall_unitary_target_and_projected_gradient(linear_func ufunc, void* udata,
+	const struct matchgate vlist[], const int nlayers, const int nqubits, const int* perms[],
+	numeric* fval, double* grad_vec);
+
+/* Per-gate Hessian of a general circuit: hess is (8*ngates)^2 complex, row g*8+x,
+ * column h*8+y (x, y: 0..3 center, 4..7 corner), same conventions as the per-layer
+ * Hessian of matchgate_brickwall_unitary_target_gradient_hessian. */
+int matchgate_circuit_unitary_target_gradient_hessian(linear_func ufunc, void* udata,
+	const struct matchgate gates[], const int ngates, const int wires[], const int nqubits,
+	numeric* fval, struct matchgate dgates[], numeric* hess);
+
+/* Partial traces over the basis columns b in [col_begin, col_end): the column range
+ * the reference gives each MPI rank (benchmark_hpc/benchmark_mpi.c:26-45).  Summing
+ * the results of disjoint ranges gives the full trace. */
+int mg_brickwall_target_and_gradient_columns(linear_func ufunc, void* udata,
+	const struct matchgate vlist[], const int nlayers, const int nqubits, const int* perms[],
+	long col_begin, long col_end, numeric* fval, struct matchgate dvlist[]);
+
+/* ---------------------------------------------------------------------------------
+ * Device-resident evaluation plans: build once, then re-evaluate with new gates
+ * without re-planning.  `what` is MG_EVAL_TARGET, MG_EVAL_GRADIENT or
+ * MG_EVAL_HESSIAN (| MG_EVAL_TI for the translation-invariant Hessian).
+ * mg_plan_run leaves the results on the GPU; mg_plan_results copies them out.
+ * --------------------------------------------------------------------------------- */
+enum { MG_EVAL_TARGET = 0, MG_EVAL_GRADIENT = 1, MG_EVAL_HESSIAN = 2, MG_EVAL_TI = 4 };
+typedef struct mg_plan mg_plan;
+mg_plan* mg_plan_brickwall(linear_func ufunc, void* udata, const struct matchgate vlist[], int nlayers, int nqubits,
+	const int* perms[], int what);
+int mg_plan_set_gates(mg_plan* plan, const struct matchgate vlist[]);
+int mg_plan_run(mg_plan* plan);
+/* any output pointer may be NULL; grad_vec/H are the projected (Riemannian) forms */
+int mg_plan_results(mg_plan* plan, numeric* fval, struct matchgate dvlist[], numeric* hess, double* grad_vec, double* H);
+void mg_plan_free(mg_plan* plan);
+/* GPU time of `steps` back-to-back mg_plan_run calls measured with CUDA events on the
+ * library's stream; when flush_l2 != 0 a buffer larger than L2 is written between
+ * runs, outside the timed intervals.  Returns the summed milliseconds (< 0 on error). */
+double mg_plan_time_ms(mg_plan* plan, int steps, int flush_l2);
+/* Number of kernels this library has launched since it was loaded. */
+long mg_launch_count(void);
+/* Peak FP32 FMA rate of this GPU, measured by a dependent-FMA kernel of this library
+ * (GFLOP/s, 2 flops per FMA); used as the roofline denominator of the FP32 pipe. */
+double mg_measure_fp32_peak_gflops(void);
+double mg_measure_fp64_peak_gflops(void);
+
+#ifdef __cplusplus
+}
+#endif

@@ -1,0 +1,1250 @@
+// Batched evaluation of f = -tr(U^dagger W), its gate gradients and its Hessian on
+// the GPU: the trace over basis columns b (reference src/matchgate_target.c:397-513),
+// one column per thread block at a time, all columns of a call in one launch.
+//
+// Parity sectors.  Every matchgate preserves the parity of the basis index, so the
+// column W e_b lives in the 2^(L-1) amplitudes of b's parity sector, and so do all
+// forward and backward states that contribute to f, the gradient or the Hessian
+// (amplitudes of the other sector only ever meet zeros).  A sector amplitude with
+// full index a is stored at compact index c = a >> 1; the dropped least significant
+// bit (qubit L-1) follows from the parity.  Qubit q < L-1 is compact bit L-2-q.
+// Each gate then maps, for every compact "quartet", one corner pair (x, w) with its
+// corner block and one center pair (y, z) with its center block.
+//
+// Tiles and passes.  A column's sector lives in a per-block global slot.  A pass
+// loads tiles of 2^kt amplitudes spanning kt "local" compact bits into shared
+// memory, applies every gate of the pass whose bits are local, and stores the tile
+// back; when the sector has at most kt bits there is one tile and one pass.  The
+// host schedules the passes: target circuits are greedily reordered (commuting gates
+// only) to fuse many gates per pass; the fitted circuit W keeps its order, so the
+// Hessian's "later gate" relation is the reference's.
+#include "mgcu_common.cuh"
+
+#include <algorithm>
+#include <vector>
+
+namespace {
+
+constexpr int MAXKT = 14;   // at most 2^14 amplitudes per shared-memory tile
+constexpr int MAXNB = 31;   // compact bits (L <= 32)
+
+struct PassRec
+{
+	int gbeg, gend;        // this pass's gates: GateRec[gbeg, gend)
+	int nnl;               // number of nonlocal compact bits (tiles = 2^nnl)
+	int lbits[MAXKT];      // local bit j -> compact bit
+	int nlbits[MAXNB];     // nonlocal bits, ascending
+};
+
+// type 0: both wires compact (la: wire i, lb: wire j); type 1: wire j is the
+// dropped qubit (la: wire i); type 2: wire i is the dropped qubit (lb: wire j).
+// lc: an auxiliary local bit used to pair a corner and a center pair.
+struct GateRec { int g, type, la, lb, lc; };
+
+struct Sched
+{
+	std::vector<PassRec> pass;
+	std::vector<GateRec> gate;
+	std::vector<int> pass_of;   // gate -> pass
+};
+
+int compact_bit(int L, int q) { return q == L - 1 ? -1 : L - 2 - q; }
+
+// Build the pass schedule of a gate sequence.  reorder = false keeps the sequential
+// order (passes are contiguous runs); reorder = true greedily pulls ready gates (all
+// earlier gates on both wires scheduled) that add the fewest new local bits.
+void schedule(int L, int kt, const int* wires, int ng, bool reorder, Sched& s)
+{
+	const int nb = L - 1;
+	const int c0 = std::min(3, kt);
+	s.pass.clear(); s.gate.clear(); s.pass_of.assign(ng, -1);
+
+	std::vector<int> order;
+	std::vector<std::vector<int>> passes_gates;
+	std::vector<unsigned> passes_sets;
+	auto bits_of = [&](int g) {
+		unsigned m = 0;
+		const int a = compact_bit(L, wires[2 * g]), b = compact_bit(L, wires[2 * g + 1]);
+		if (a >= 0) m |= 1u << a;
+		if (b >= 0) m |= 1u << b;
+		return m;
+	};
+	const unsigned base_set = (nb <= kt) ? ((nb >= 32) ? 0xffffffffu : ((1u << nb) - 1)) : ((1u << c0) - 1);
+
+	if (!reorder)
+	{
+		unsigned cur = base_set;
+		std::vector<int> pg;
+		for (int g = 0; g < ng; g++)
+		{
+			const unsigned nm = cur | bits_of(g);
+			if (__builtin_popcount(nm) > kt && !pg.empty())
+			{
+				passes_gates.push_back(pg); passes_sets.push_back(cur);
+				pg.clear(); cur = base_set | bits_of(g);
+			}
+			else cur = nm;
+			pg.push_back(g);
+		}
+		passes_gates.push_back(pg); passes_sets.push_back(cur);
+	}
+	else
+	{
+		std::vector<std::vector<int>> onq(L);
+		for (int g = 0; g < ng; g++) { onq[wires[2 * g]].push_back(g); onq[wires[2 * g + 1]].push_back(g); }
+		std::vector<size_t> fr(L, 0);
+		int done = 0;
+		while (done < ng || passes_gates.empty())
+		{
+			unsigned cur = base_set;
+			std::vector<int> pg;
+			for (;;)
+			{
+				int best = -1, bestnew = 99;
+				for (int q = 0; q < L; q++)
+				{
+					if (fr[q] >= onq[q].size()) continue;
+					const int g = onq[q][fr[q]];
+					const int q2 = (wires[2 * g] == q) ? wires[2 * g + 1] : wires[2 * g];
+					if (fr[q2] >= onq[q2].size() || onq[q2][fr[q2]] != g) continue;
+					const unsigned m = bits_of(g);
+					const int nw = __builtin_popcount(m & ~cur);
+					if (__builtin_popcount(cur | m) > kt) continue;
+					if (nw < bestnew || (nw == bestnew && g < best)) { best = g; bestnew = nw; }
+				}
+				if (best < 0) break;
+				cur |= bits_of(best);
+				fr[wires[2 * best]]++; fr[wires[2 * best + 1]]++;
+				pg.push_back(best);
+				done++;
+			}
+			passes_gates.push_back(pg); passes_sets.push_back(cur);
+			if (pg.empty()) break;   // only for ng == 0
+		}
+	}
+
+	for (size_t p = 0; p < passes_gates.size(); p++)
+	{
+		unsigned set = passes_sets[p];
+		// pad the local set to kt bits with the lowest unused compact bits
+		for (int b = 0; b < nb && __builtin_popcount(set) < std::min(kt, nb); b++) set |= 1u << b;
+		PassRec pr;
+		memset(&pr, 0, sizeof(pr));
+		int nl = 0, nn = 0;
+		int lpos[32];
+		for (int b = 0; b < nb; b++)
+		{
+			if (set & (1u << b)) { lpos[b] = nl; pr.lbits[nl++] = b; }
+			else { lpos[b] = -1; pr.nlbits[nn++] = b; }
+		}
+		pr.nnl = nn;
+		pr.gbeg = (int)s.gate.size();
+		for (int g : passes_gates[p])
+		{
+			GateRec r;
+			const int a = compact_bit(L, wires[2 * g]), b = compact_bit(L, wires[2 * g + 1]);
+			r.g = g;
+			r.type = (a >= 0 && b >= 0) ? 0 : (b < 0 ? 1 : 2);
+			r.la = a >= 0 ? lpos[a] : -1;
+			r.lb = b >= 0 ? lpos[b] : -1;
+			const int used = r.type == 1 ? r.la : r.lb;
+			r.lc = (used == 0) ? 1 : 0;
+			s.gate.push_back(r);
+			s.pass_of[g] = (int)p;
+		}
+		pr.gend = (int)s.gate.size();
+		s.pass.push_back(pr);
+	}
+}
+
+// ------------------------------------------------------------------------------------
+// device side
+// ------------------------------------------------------------------------------------
+
+__device__ __forceinline__ unsigned ins0u(unsigned t, int p) { return ((t >> p) << (p + 1)) | (t & ((1u << p) - 1u)); }
+
+struct ProgDev
+{
+	const PassRec* pass;
+	const GateRec* gate;
+	int npass;
+};
+
+template <class P>
+struct Args
+{
+	typedef typename P::T T;
+	int L, nb, kt;
+	long S;                    // 2^(L-1)
+	ProgDev W, U;
+	const T* wm;               // W gate matrices [ngates][8]: c0..c3, k0..k3
+	const T* um;               // target gate matrices
+	int ngates;
+	const T* dense;            // -conj(U e_b) columns, or null (then U is run)
+	long dense_b0;
+	long b0, b1;               // column range of this launch
+	T* su;                     // per-block slots [grid][S]
+	T* sw;
+	T* cache;                  // forward inputs per gate
+	T* dcache;                 // backward inputs per gate (Hessian)
+	int cache_per_column;      // 1: cache slot b - b0, 0: slot blockIdx.x
+	int want_grad;
+	double* part_f;            // [grid][2]
+	double* part_g;            // [grid][ngates][16]
+	// Hessian
+	const int* place;
+	const double* place_w;     // [nplace][ngates]
+	const int* pass_of;
+	const int* block;          // [ngates]
+	int nplace, mdim;          // mdim = 8 * nblocks
+	double* part_h;            // [grid][mdim][mdim][2]
+	T* sh;                     // per-block slot for placeholder states
+	T* ucols;                  // target-only launch: output columns [b - b0][S]
+};
+
+// shared-memory layout: tile, then the two deposit tables, then reduction scratch
+struct Smem
+{
+	unsigned* dlo;
+	unsigned* dhi;
+	double* red;
+	int h;
+};
+
+template <class T>
+__device__ __forceinline__ Smem smem_layout(char* base, int kt, T*& tile)
+{
+	Smem s;
+	tile = reinterpret_cast<T*>(base);
+	s.dlo = reinterpret_cast<unsigned*>(base + sizeof(T) * (1u << kt));
+	s.dhi = s.dlo + 128;
+	s.red = reinterpret_cast<double*>(s.dhi + 128);
+	s.h = kt / 2;
+	return s;
+}
+
+// local -> compact index tables for one pass (caller synchronises)
+__device__ __forceinline__ void setup_pass(const PassRec& pr, int kt, Smem& s)
+{
+	const int h = s.h;
+	for (int i = threadIdx.x; i < 128; i += blockDim.x)
+	{
+		unsigned lo = 0, hi = 0;
+		for (int j = 0; j < h; j++) if (i & (1 << j)) lo |= 1u << pr.lbits[j];
+		for (int j = 0; j < kt - h; j++) if (i & (1 << j)) hi |= 1u << pr.lbits[h + j];
+		s.dlo[i] = lo;
+		s.dhi[i] = hi;
+	}
+}
+
+__device__ __forceinline__ unsigned nl_base(const PassRec& pr, unsigned tau)
+{
+	unsigned b = 0;
+	for (int j = 0; j < pr.nnl; j++) if (tau & (1u << j)) b |= 1u << pr.nlbits[j];
+	return b;
+}
+
+__device__ __forceinline__ unsigned gidx(const Smem& s, unsigned base, unsigned e)
+{
+	return base | s.dlo[e & ((1u << s.h) - 1u)] | s.dhi[e >> s.h];
+}
+
+// quartet q of a gate -> tile positions of x, w (corner pair) and y, z (center pair)
+__device__ __forceinline__ void quartet(const GateRec& r, unsigned q, int tpar, unsigned& ex, unsigned& ew, unsigned& ey, unsigned& ez)
+{
+	if (r.type == 0)
+	{
+		const int lo = min(r.la, r.lb), hi = max(r.la, r.lb);
+		const unsigned base = ins0u(ins0u(q, lo), hi);
+		const unsigned A = 1u << r.la, B = 1u << r.lb;
+		ex = base; ew = base | A | B; ey = base | B; ez = base | A;
+	}
+	else
+	{
+		const int l = (r.type == 1) ? r.la : r.lb;
+		const int lo = min(l, r.lc), hi = max(l, r.lc);
+		const unsigned base = ins0u(ins0u(q, lo), hi);
+		const unsigned A = 1u << l, C = 1u << r.lc;
+		const int s = (__popc(base) + tpar) & 1;   // dropped bit of the base amplitude
+		if (r.type == 1)
+		{
+			const unsigned a0 = base, a1 = base | A, b0 = base | C, b1 = base | C | A;
+			ex = s ? b0 : a0; ew = s ? b1 : a1; ey = s ? a0 : b0; ez = s ? a1 : b1;
+		}
+		else
+		{
+			ex = s ? (base | C) : base;
+			ew = s ? (base | C | A) : (base | A);
+			ey = s ? (base | A) : (base | C | A);
+			ez = s ? base : (base | C);
+		}
+	}
+}
+
+template <class P> struct Red;
+template <> struct Red<PrecD>
+{
+	typedef double R;
+	__device__ static void split(const PrecD::Acc& a, R& re, R& im) { re = a.re; im = a.im; }
+	__device__ static void add(R& a, R b) { a += b; }
+	__device__ static R shfl(R a, int m) { return __shfl_xor_sync(0xffffffffu, a, m); }
+	__device__ static double to_d(R a) { return a; }
+};
+template <> struct Red<PrecF>
+{
+	typedef float2 R;
+	__device__ static void split(const PrecF::Acc& a, R& re, R& im) { re = make_float2(a.rh, a.rl); im = make_float2(a.ih, a.il); }
+	__device__ static void add(R& a, R b) { ff_add(a.x, a.y, b.x, b.y); }
+	__device__ static R shfl(R a, int m) { return make_float2(__shfl_xor_sync(0xffffffffu, a.x, m), __shfl_xor_sync(0xffffffffu, a.y, m)); }
+	__device__ static double to_d(R a) { return (double)a.x + (double)a.y; }
+};
+template <> struct Red<PrecX> : Red<PrecF> {};
+
+// Reduce 8 complex accumulators over the block and add w * (sum) to dst[0..15]
+// (re, im interleaved).  Warp level: a reduce-scatter over 16 reals (16 adds per
+// lane instead of 80); block level: fixed-order FP64 sums over warps.
+template <class P>
+__device__ void block_reduce8(const typename P::Acc (&a)[8], double* red, double* dst, double w)
+{
+	typedef Red<P> RD;
+	typename RD::R v[16];
+#pragma unroll
+	for (int e = 0; e < 8; e++) RD::split(a[e], v[2 * e], v[2 * e + 1]);
+	const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+#pragma unroll
+	for (int t = 0; t < 8; t++)
+	{
+		const bool up = lane & 16;
+		typename RD::R send = up ? v[t] : v[t + 8], keep = up ? v[t + 8] : v[t];
+		RD::add(keep, RD::shfl(send, 16));
+		v[t] = keep;
+	}
+#pragma unroll
+	for (int t = 0; t < 4; t++)
+	{
+		const bool up = lane & 8;
+		typename RD::R send = up ? v[t] : v[t + 4], keep = up ? v[t + 4] : v[t];
+		RD::add(keep, RD::shfl(send, 8));
+		v[t] = keep;
+	}
+#pragma unroll
+	for (int t = 0; t < 2; t++)
+	{
+		const bool up = lane & 4;
+		typename RD::R send = up ? v[t] : v[t + 2], keep = up ? v[t + 2] : v[t];
+		RD::add(keep, RD::shfl(send, 4));
+		v[t] = keep;
+	}
+	{
+		const bool up = lane & 2;
+		typename RD::R send = up ? v[0] : v[1], keep = up ? v[1] : v[0];
+		RD::add(keep, RD::shfl(send, 2));
+		v[0] = keep;
+	}
+	RD::add(v[0], RD::shfl(v[0], 1));
+	const int idx = ((lane >> 4) & 1) * 8 + ((lane >> 3) & 1) * 4 + ((lane >> 2) & 1) * 2 + ((lane >> 1) & 1);
+	if ((lane & 1) == 0) red[warp * 16 + idx] = RD::to_d(v[0]);
+	__syncthreads();
+	if (threadIdx.x < 16)
+	{
+		double s = 0;
+		const int nw = blockDim.x >> 5;
+		for (int k = 0; k < nw; k++) s += red[k * 16 + threadIdx.x];
+		dst[threadIdx.x] += w * s;
+	}
+	__syncthreads();
+}
+
+template <class P>
+__device__ void block_reduce1(const typename P::Acc& a, double* red, double* dst)
+{
+	typedef Red<P> RD;
+	typename RD::R re, im;
+	RD::split(a, re, im);
+	for (int m = 16; m > 0; m >>= 1) { RD::add(re, RD::shfl(re, m)); RD::add(im, RD::shfl(im, m)); }
+	const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+	if (lane == 0) { red[warp * 2] = RD::to_d(re); red[warp * 2 + 1] = RD::to_d(im); }
+	__syncthreads();
+	if (threadIdx.x < 2)
+	{
+		double s = 0;
+		for (int k = 0; k < (int)(blockDim.x >> 5); k++) s += red[k * 2 + threadIdx.x];
+		dst[threadIdx.x] += s;
+	}
+	__syncthreads();
+}
+
+template <class T>
+struct Gate8 { T c0, c1, c2, c3, k0, k1, k2, k3; };
+
+template <class T>
+__device__ __forceinline__ Gate8<T> load_gate(const T* m, int g)
+{
+	Gate8<T> r;
+	const T* p = m + (size_t)g * 8;
+	r.c0 = p[0]; r.c1 = p[1]; r.c2 = p[2]; r.c3 = p[3];
+	r.k0 = p[4]; r.k1 = p[5]; r.k2 = p[6]; r.k3 = p[7];
+	return r;
+}
+
+// apply one gate to the tile (forward); optionally store each input amplitude to
+// the gate's cache column first
+template <class P>
+__device__ __forceinline__ void gate_forward(typename P::T* tile, const GateRec& r, const Gate8<typename P::T>& G, int Q, int tpar,
+	typename P::T* cache_g, const Smem& s, unsigned nlb)
+{
+	for (unsigned q = threadIdx.x; q < (unsigned)Q; q += blockDim.x)
+	{
+		unsigned ex, ew, ey, ez;
+		quartet(r, q, tpar, ex, ew, ey, ez);
+		const typename P::T x = tile[ex], w = tile[ew], y = tile[ey], z = tile[ez];
+		if (cache_g)
+		{
+			cache_g[gidx(s, nlb, ex)] = x; cache_g[gidx(s, nlb, ew)] = w;
+			cache_g[gidx(s, nlb, ey)] = y; cache_g[gidx(s, nlb, ez)] = z;
+		}
+		tile[ex] = P::madd2(G.k0, x, G.k1, w);
+		tile[ew] = P::madd2(G.k2, x, G.k3, w);
+		tile[ey] = P::madd2(G.c0, y, G.c1, z);
+		tile[ez] = P::madd2(G.c2, y, G.c3, z);
+	}
+}
+
+// contraction of the derivative d (state after the gate, read from dsrc) with the
+// state before the gate x: acc[e] += d_r x_s for the 8 block entries
+template <class P>
+__device__ __forceinline__ void contract_quartet(typename P::Acc (&acc)[8], typename P::T dx, typename P::T dw, typename P::T dy, typename P::T dz,
+	typename P::T x, typename P::T w, typename P::T y, typename P::T z)
+{
+	P::acc_mul_add(acc[0], dy, y); P::acc_mul_add(acc[1], dy, z);
+	P::acc_mul_add(acc[2], dz, y); P::acc_mul_add(acc[3], dz, z);
+	P::acc_mul_add(acc[4], dx, x); P::acc_mul_add(acc[5], dx, w);
+	P::acc_mul_add(acc[6], dw, x); P::acc_mul_add(acc[7], dw, w);
+}
+
+// ---- tile transfers ----
+template <class P>
+__device__ __forceinline__ void tile_load_basis(typename P::T* tile, int kt, const Smem& s, unsigned nlb, unsigned cb)
+{
+	for (unsigned e = threadIdx.x; e < (1u << kt); e += blockDim.x)
+		tile[e] = (gidx(s, nlb, e) == cb) ? P::make(1.0, 0.0) : P::zero();
+}
+
+template <class P>
+__device__ __forceinline__ void tile_load(typename P::T* tile, int kt, const Smem& s, unsigned nlb, const typename P::T* src)
+{
+	for (unsigned e = threadIdx.x; e < (1u << kt); e += blockDim.x) tile[e] = src[gidx(s, nlb, e)];
+}
+
+template <class P>
+__device__ __forceinline__ void tile_store(const typename P::T* tile, int kt, const Smem& s, unsigned nlb, typename P::T* dst, bool negconj)
+{
+	for (unsigned e = threadIdx.x; e < (1u << kt); e += blockDim.x)
+	{
+		const typename P::T v = tile[e];
+		dst[gidx(s, nlb, e)] = negconj ? P::negconj(v) : v;
+	}
+}
+
+// run a forward program from e_cb into `slot` (the result, -conj'ed if requested,
+// ends in slot)
+template <class P>
+__device__ void run_forward(const ProgDev& prog, const typename P::T* mats, int kt, int nb, int par, unsigned cb,
+	typename P::T* tile, Smem& s, typename P::T* slot, bool negconj_end)
+{
+	const int Q = 1 << (kt - 2);
+	for (int p = 0; p < prog.npass; p++)
+	{
+		const PassRec& pr = prog.pass[p];
+		__syncthreads();
+		setup_pass(pr, kt, s);
+		__syncthreads();
+		const unsigned ntile = 1u << pr.nnl;
+		for (unsigned tau = 0; tau < ntile; tau++)
+		{
+			const unsigned nlb = nl_base(pr, tau);
+			const int tpar = (__popc(nlb) + par) & 1;
+			if (p == 0) tile_load_basis<P>(tile, kt, s, nlb, cb);
+			else tile_load<P>(tile, kt, s, nlb, slot);
+			__syncthreads();
+			for (int gi = pr.gbeg; gi < pr.gend; gi++)
+			{
+				const GateRec r = prog.gate[gi];
+				const Gate8<typename P::T> G = load_gate(mats, r.g);
+				gate_forward<P>(tile, r, G, Q, tpar, nullptr, s, nlb);
+				__syncthreads();
+			}
+			tile_store<P>(tile, kt, s, nlb, slot, negconj_end && p == prog.npass - 1);
+			__syncthreads();
+		}
+	}
+}
+
+// ------------------------------------------------------------------------------------
+// stage A: per column -- target, W forward with cache, overlap, W backward
+// ------------------------------------------------------------------------------------
+template <class P>
+__global__ void __launch_bounds__(256) k_columns(Args<P> a)
+{
+	typedef typename P::T T;
+	extern __shared__ __align__(16) char smem_raw[];
+	T* tile;
+	Smem s = smem_layout<T>(smem_raw, a.kt, tile);
+	const int kt = a.kt, Q = 1 << (kt - 2);
+	const long S = a.S;
+	typename P::Acc facc = P::acc_zero();
+	T* su = a.su + (size_t)blockIdx.x * S;
+	T* sw = a.sw + (size_t)blockIdx.x * S;
+
+	for (long b = a.b0 + blockIdx.x; b < a.b1; b += gridDim.x)
+	{
+		const int par = __popcll(b) & 1;
+		const unsigned cb = (unsigned)(b >> 1);
+		const T* dsrc;
+		if (a.dense) dsrc = a.dense + (size_t)(b - a.dense_b0) * S;
+		else
+		{
+			run_forward<P>(a.U, a.um, kt, a.nb, par, cb, tile, s, su, true);
+			dsrc = su;
+		}
+		if (a.ucols)
+		{
+			// target-only launch: keep -conj(U e_b)
+			T* out = a.ucols + (size_t)(b - a.b0) * S;
+			for (long e = threadIdx.x; e < S; e += blockDim.x) out[e] = su[e];
+			__syncthreads();
+			continue;
+		}
+		const long slot = a.cache_per_column ? (b - a.b0) : blockIdx.x;
+		T* cache = a.cache ? a.cache + (size_t)slot * a.ngates * S : nullptr;
+		T* dcache = a.dcache ? a.dcache + (size_t)slot * a.ngates * S : nullptr;
+
+		// W forward, caching each gate's input; overlap on the last pass
+		for (int p = 0; p < a.W.npass; p++)
+		{
+			const PassRec& pr = a.W.pass[p];
+			__syncthreads();
+			setup_pass(pr, kt, s);
+			__syncthreads();
+			const unsigned ntile = 1u << pr.nnl;
+			const bool last = (p == a.W.npass - 1);
+			for (unsigned tau = 0; tau < ntile; tau++)
+			{
+				const unsigned nlb = nl_base(pr, tau);
+				const int tpar = (__popcll(nlb) + par) & 1;
+				if (p == 0) tile_load_basis<P>(tile, kt, s, nlb, cb);
+				else tile_load<P>(tile, kt, s, nlb, sw);
+				__syncthreads();
+				for (int gi = pr.gbeg; gi < pr.gend; gi++)
+				{
+					const GateRec r = a.W.gate[gi];
+					const Gate8<T> G = load_gate(a.wm, r.g);
+					gate_forward<P>(tile, r, G, Q, tpar, cache ? cache + (size_t)r.g * S : nullptr, s, nlb);
+					__syncthreads();
+				}
+				if (last)
+				{
+					for (unsigned e = threadIdx.x; e < (1u << kt); e += blockDim.x)
+						P::acc_mul_add(facc, dsrc[gidx(s, nlb, e)], tile[e]);
+				}
+				else tile_store<P>(tile, kt, s, nlb, sw, false);
+				__syncthreads();
+			}
+		}
+
+		if (!a.want_grad) continue;
+
+		// W backward: tile holds the derivative after the gate
+		for (int p = a.W.npass - 1; p >= 0; p--)
+		{
+			const PassRec& pr = a.W.pass[p];
+			__syncthreads();
+			setup_pass(pr, kt, s);
+			__syncthreads();
+			const unsigned ntile = 1u << pr.nnl;
+			for (unsigned tau = 0; tau < ntile; tau++)
+			{
+				const unsigned nlb = nl_base(pr, tau);
+				const int tpar = (__popcll(nlb) + par) & 1;
+				tile_load<P>(tile, kt, s, nlb, (p == a.W.npass - 1) ? dsrc : su);
+				__syncthreads();
+				for (int gi = pr.gend - 1; gi >= pr.gbeg; gi--)
+				{
+					const GateRec r = a.W.gate[gi];
+					const Gate8<T> G = load_gate(a.wm, r.g);
+					const T* cg = cache + (size_t)r.g * S;
+					T* dg = dcache ? dcache + (size_t)r.g * S : nullptr;
+					typename P::Acc acc[8];
+#pragma unroll
+					for (int e = 0; e < 8; e++) acc[e] = P::acc_zero();
+					for (unsigned q = threadIdx.x; q < (unsigned)Q; q += blockDim.x)
+					{
+						unsigned ex, ew, ey, ez;
+						quartet(r, q, tpar, ex, ew, ey, ez);
+						const unsigned gx = gidx(s, nlb, ex), gw = gidx(s, nlb, ew), gy = gidx(s, nlb, ey), gz = gidx(s, nlb, ez);
+						const T dx = tile[ex], dw = tile[ew], dy = tile[ey], dz = tile[ez];
+						if (dg) { dg[gx] = dx; dg[gw] = dw; dg[gy] = dy; dg[gz] = dz; }
+						contract_quartet<P>(acc, dx, dw, dy, dz, cg[gx], cg[gw], cg[gy], cg[gz]);
+						// transpose (no conjugation): reference src/gate.c:725-728
+						tile[ex] = P::madd2(G.k0, dx, G.k2, dw);
+						tile[ew] = P::madd2(G.k1, dx, G.k3, dw);
+						tile[ey] = P::madd2(G.c0, dy, G.c2, dz);
+						tile[ez] = P::madd2(G.c1, dy, G.c3, dz);
+					}
+					block_reduce8<P>(acc, s.red, a.part_g + ((size_t)blockIdx.x * a.ngates + r.g) * 16, 1.0);
+				}
+				if (p > 0) tile_store<P>(tile, kt, s, nlb, su, false);
+				__syncthreads();
+			}
+		}
+	}
+	block_reduce1<P>(facc, s.red, a.part_f + (size_t)blockIdx.x * 2);
+}
+
+// ------------------------------------------------------------------------------------
+// stage B: Hessian items (column, placement, entry): the placeholder state of one
+// gate entry pushed through all later gates, contracted at each with the cached
+// derivative (reference src/matchgate_brickwall.c:177-231)
+// ------------------------------------------------------------------------------------
+template <class P>
+__global__ void __launch_bounds__(256) k_hessian(Args<P> a, long nitems)
+{
+	typedef typename P::T T;
+	extern __shared__ __align__(16) char smem_raw[];
+	T* tile;
+	Smem s = smem_layout<T>(smem_raw, a.kt, tile);
+	const int kt = a.kt, Q = 1 << (kt - 2);
+	const long S = a.S;
+	T* sh = a.sh + (size_t)blockIdx.x * S;
+	double* parth = a.part_h + (size_t)blockIdx.x * a.mdim * a.mdim * 2;
+
+	for (long it = blockIdx.x; it < nitems; it += gridDim.x)
+	{
+		const int x = (int)(it & 7);
+		const long rest = it >> 3;
+		const int p = (int)(rest % a.nplace);
+		const long bi = rest / a.nplace;
+		const long b = a.b0 + bi;
+		const int par = __popcll(b) & 1;
+		const int k = a.place[p];
+		const int pk = a.pass_of[k];
+		const T* cache = a.cache + (size_t)bi * a.ngates * S;
+		const T* dcache = a.dcache + (size_t)bi * a.ngates * S;
+		const double* wrow = a.place_w + (size_t)p * a.ngates;
+		double* hrow = parth + (size_t)(a.block[k] * 8 + x) * a.mdim * 2;
+		for (int pp = pk; pp < a.W.npass; pp++)
+		{
+			const PassRec& pr = a.W.pass[pp];
+			__syncthreads();
+			setup_pass(pr, kt, s);
+			__syncthreads();
+			const unsigned ntile = 1u << pr.nnl;
+			for (unsigned tau = 0; tau < ntile; tau++)
+			{
+				const unsigned nlb = nl_base(pr, tau);
+				const int tpar = (__popcll(nlb) + par) & 1;
+				tile_load<P>(tile, kt, s, nlb, (pp == pk) ? cache + (size_t)k * S : sh);
+				__syncthreads();
+				for (int gi = pr.gbeg; gi < pr.gend; gi++)
+				{
+					const GateRec r = a.W.gate[gi];
+					if (r.g < k) continue;
+					if (r.g == k)
+					{
+						// placeholder: the derivative of the gate's output w.r.t. entry x
+						for (unsigned q = threadIdx.x; q < (unsigned)Q; q += blockDim.x)
+						{
+							unsigned ex, ew, ey, ez;
+							quartet(r, q, tpar, ex, ew, ey, ez);
+							const T vx = tile[ex], vw = tile[ew], vy = tile[ey], vz = tile[ez];
+							const T zero = P::zero();
+							T ox = zero, ow = zero, oy = zero, oz = zero;
+							switch (x)
+							{
+							case 0: oy = vy; break;   // center (0,0)
+							case 1: oy = vz; break;   // center (0,1)
+							case 2: oz = vy; break;   // center (1,0)
+							case 3: oz = vz; break;   // center (1,1)
+							case 4: ox = vx; break;   // corner (0,0)
+							case 5: ox = vw; break;   // corner (0,1)
+							case 6: ow = vx; break;   // corner (1,0)
+							default: ow = vw; break;  // corner (1,1)
+							}
+							tile[ex] = ox; tile[ew] = ow; tile[ey] = oy; tile[ez] = oz;
+						}
+						__syncthreads();
+						continue;
+					}
+					const Gate8<T> G = load_gate(a.wm, r.g);
+					const T* dg = dcache + (size_t)r.g * S;
+					const bool apply = (r.g != a.ngates - 1);
+					typename P::Acc acc[8];
+#pragma unroll
+					for (int e = 0; e < 8; e++) acc[e] = P::acc_zero();
+					for (unsigned q = threadIdx.x; q < (unsigned)Q; q += blockDim.x)
+					{
+						unsigned ex, ew, ey, ez;
+						quartet(r, q, tpar, ex, ew, ey, ez);
+						const T vx = tile[ex], vw = tile[ew], vy = tile[ey], vz = tile[ez];
+						contract_quartet<P>(acc, dg[gidx(s, nlb, ex)], dg[gidx(s, nlb, ew)], dg[gidx(s, nlb, ey)], dg[gidx(s, nlb, ez)], vx, vw, vy, vz);
+						if (apply)
+						{
+							tile[ex] = P::madd2(G.k0, vx, G.k1, vw);
+							tile[ew] = P::madd2(G.k2, vx, G.k3, vw);
+							tile[ey] = P::madd2(G.c0, vy, G.c1, vz);
+							tile[ez] = P::madd2(G.c2, vy, G.c3, vz);
+						}
+					}
+					block_reduce8<P>(acc, s.red, hrow + (size_t)a.block[r.g] * 16, wrow[r.g]);
+				}
+				if (pp < a.W.npass - 1) tile_store<P>(tile, kt, s, nlb, sh, false);
+				__syncthreads();
+			}
+		}
+	}
+}
+
+// ------------------------------------------------------------------------------------
+// small kernels: staging, reductions, symmetrisation
+// ------------------------------------------------------------------------------------
+
+// dense target U (row-major 2^L x 2^L, FP64) -> -conj(U e_b) on b's sector, [b - b0][S]
+template <class P>
+__global__ void k_dense_columns(const double2* __restrict__ U, int L, long b0, long b1, typename P::T* __restrict__ out)
+{
+	const long S = 1L << (L - 1), n = 1L << L;
+	const long total = (b1 - b0) * S;
+	for (long u = blockIdx.x * (long)blockDim.x + threadIdx.x; u < total; u += (long)gridDim.x * blockDim.x)
+	{
+		const long bi = u / S, c = u - bi * S;
+		const long b = b0 + bi;
+		const int par = (__popcll(b) + __popcll(c)) & 1;
+		const long arow = (c << 1) | par;
+		const double2 v = U[arow * n + b];
+		out[u] = P::make(-v.x, v.y);
+	}
+}
+
+// host-supplied FP64 sector columns -> precision T
+template <class P>
+__global__ void k_convert(const double2* __restrict__ in, long n, typename P::T* __restrict__ out)
+{
+	for (long u = blockIdx.x * (long)blockDim.x + threadIdx.x; u < n; u += (long)gridDim.x * blockDim.x)
+		out[u] = P::make(in[u].x, in[u].y);
+}
+
+// out[r] = sum over parts (fixed order) of part[c * len + r]
+__global__ void k_sum_parts(const double* __restrict__ part, int nparts, long len, double* __restrict__ out)
+{
+	for (long r = blockIdx.x * (long)blockDim.x + threadIdx.x; r < len; r += (long)gridDim.x * blockDim.x)
+	{
+		double s = 0;
+		for (int c = 0; c < nparts; c++) s += part[(size_t)c * len + r];
+		out[r] = s;
+	}
+}
+
+// per-gate gradients [ngates][16] -> per-block sums [nblocks][16], gates in order
+__global__ void k_block_sum(const double* __restrict__ g, const int* __restrict__ block, int ngates, int nblocks, double* __restrict__ out)
+{
+	const int t = blockIdx.x * blockDim.x + threadIdx.x;
+	if (t >= nblocks * 16) return;
+	const int blk = t / 16, v = t % 16;
+	double s = 0;
+	for (int q = 0; q < ngates; q++) if (block[q] == blk) s += g[q * 16 + v];
+	out[t] = s;
+}
+
+// diagonal blocks A -> A + A^T, then (second kernel) lower blocks mirrored from upper
+__global__ void k_symm_diag(int nb, double2* __restrict__ h)
+{
+	const int m = nb * 8;
+	for (int q = blockIdx.x * blockDim.x + threadIdx.x; q < m * m; q += gridDim.x * blockDim.x)
+	{
+		const int r = q / m, c = q % m;
+		if (r / 8 != c / 8) continue;
+		if (c % 8 < r % 8)
+		{
+			const double2 a = h[(long)r * m + c], b = h[(long)c * m + r];
+			const double2 s = make_double2(a.x + b.x, a.y + b.y);
+			h[(long)r * m + c] = s; h[(long)c * m + r] = s;
+		}
+		else if (c % 8 == r % 8) { h[(long)r * m + c].x *= 2; h[(long)r * m + c].y *= 2; }
+	}
+}
+
+__global__ void k_mirror(int nb, double2* __restrict__ h)
+{
+	const int m = nb * 8;
+	for (int q = blockIdx.x * blockDim.x + threadIdx.x; q < m * m; q += gridDim.x * blockDim.x)
+	{
+		const int r = q / m, c = q % m;
+		if (c / 8 < r / 8) h[(long)r * m + c] = h[(long)c * m + r];
+	}
+}
+
+int grid_cap(long work, int threads)
+{
+	long b = (work + threads - 1) / threads;
+	const long cap = (long)mgcu_ctx()->nsm * 8;
+	return (int)std::max(1L, std::min(b, cap));
+}
+
+}  // namespace
+
+// ======================================================================================
+// targets
+// ======================================================================================
+struct TargetProg
+{
+	int kt = -1, prec = -1;
+	Sched sched;
+	DevBuf pass, gate, mats;
+};
+
+struct mgcu_target
+{
+	int L;
+	int kind;                      // 0 circuit, 1 dense
+	std::vector<mgg> gates;
+	std::vector<int> wires;
+	DevBuf dense;                  // FP64 U on the device
+	TargetProg progs[3];           // per precision
+	int resident = 0;
+	DevBuf res_cols[3];            // resident -conj(U e_b) per precision
+	int res_kt[3] = { -1, -1, -1 };
+	bool res_valid[3] = { false, false, false };
+};
+
+template <class P>
+static int upload_mats(const mgg* gates, int ng, DevBuf& buf)
+{
+	typedef typename P::T T;
+	std::vector<T> h((size_t)std::max(ng, 1) * 8);
+	for (int g = 0; g < ng; g++)
+		for (int q = 0; q < 4; q++)
+		{
+			h[(size_t)g * 8 + q] = P::make(gates[g].c[q].re, gates[g].c[q].im);
+			h[(size_t)g * 8 + 4 + q] = P::make(gates[g].k[q].re, gates[g].k[q].im);
+		}
+	int e = buf.alloc(sizeof(T) * h.size());
+	if (e) return e;
+	MGCU_TRY(cudaMemcpyAsync(buf.p, h.data(), sizeof(T) * h.size(), cudaMemcpyHostToDevice, mgcu_ctx()->stream));
+	MGCU_TRY(cudaStreamSynchronize(mgcu_ctx()->stream));
+	return 0;
+}
+
+static int upload_sched(const Sched& s, DevBuf& pass, DevBuf& gate)
+{
+	cudaStream_t st = mgcu_ctx()->stream;
+	int e = pass.alloc(sizeof(PassRec) * std::max<size_t>(s.pass.size(), 1));
+	if (e) return e;
+	e = gate.alloc(sizeof(GateRec) * std::max<size_t>(s.gate.size(), 1));
+	if (e) return e;
+	MGCU_TRY(cudaMemcpyAsync(pass.p, s.pass.data(), sizeof(PassRec) * s.pass.size(), cudaMemcpyHostToDevice, st));
+	if (!s.gate.empty()) MGCU_TRY(cudaMemcpyAsync(gate.p, s.gate.data(), sizeof(GateRec) * s.gate.size(), cudaMemcpyHostToDevice, st));
+	MGCU_TRY(cudaStreamSynchronize(st));
+	return 0;
+}
+
+template <class P>
+static int target_prog(mgcu_target* t, int kt, TargetProg*& out)
+{
+	TargetProg& tp = t->progs[P::kId];
+	if (tp.kt != kt)
+	{
+		schedule(t->L, kt, t->wires.data(), (int)t->gates.size(), true, tp.sched);
+		int e = upload_sched(tp.sched, tp.pass, tp.gate);
+		if (e) return e;
+		e = upload_mats<P>(t->gates.data(), (int)t->gates.size(), tp.mats);
+		if (e) return e;
+		tp.kt = kt;
+	}
+	out = &tp;
+	return 0;
+}
+
+extern "C" mgcu_target* mgcu_target_circuit(const mgg* gates, const int* wires, int ngates, int L)
+{
+	if (!mgcu_ctx()) return nullptr;
+	mgcu_target* t = new mgcu_target();
+	t->L = L; t->kind = 0;
+	t->gates.assign(gates, gates + ngates);
+	t->wires.assign(wires, wires + 2 * ngates);
+	return t;
+}
+
+extern "C" mgcu_target* mgcu_target_dense(const mgc* U, int L)
+{
+	if (!mgcu_ctx()) return nullptr;
+	mgcu_target* t = new mgcu_target();
+	t->L = L; t->kind = 1;
+	const size_t n = (size_t)1 << L;
+	if (t->dense.alloc(sizeof(double2) * n * n)) { delete t; return nullptr; }
+	if (cudaMemcpy(t->dense.p, U, sizeof(double2) * n * n, cudaMemcpyHostToDevice) != cudaSuccess)
+	{
+		mg_set_error("copying a dense target to the GPU failed");
+		delete t;
+		return nullptr;
+	}
+	return t;
+}
+
+extern "C" void mgcu_target_destroy(mgcu_target* t) { delete t; }
+extern "C" int mgcu_target_L(const mgcu_target* t) { return t->L; }
+extern "C" void mgcu_target_set_resident(mgcu_target* t, int enable)
+{
+	t->resident = enable;
+	if (!enable)
+		for (int i = 0; i < 3; i++) { t->res_valid[i] = false; }
+}
+
+extern "C" int mgcu_target_apply(mgcu_target* t, const mgc* psi, mgc* out)
+{
+	if (t->kind == 0)
+		return mgcu_circuit_forward(t->gates.data(), t->wires.data(), (int)t->gates.size(), t->L, psi, nullptr, out);
+	// dense: out = U psi (FP64 matrix-vector product on the GPU)
+	return mgcu_dense_matvec(t->dense.p, t->L, psi, out);
+}
+
+// ======================================================================================
+// plans
+// ======================================================================================
+struct mgcu_plan
+{
+	mgcu_plan_desc d;
+	std::vector<int> wires, block, place;
+	std::vector<double> place_w;
+	int L, nb, kt, threads, grid_a, grid_b, prec;
+	long S;
+	size_t tsize;
+	size_t smem;
+	long chunk;
+	Sched ws;
+	DevBuf d_pass, d_gate, d_mats, d_pass_of, d_block, d_place, d_placew;
+	DevBuf su, sw, sh, cache, dcache, part_f, part_g, part_h, cols64, cols;
+	DevBuf out_f, out_g, out_blk, out_h, flush;
+	int nparts_h;
+};
+
+static size_t prec_tsize(int prec) { return prec == MG_PREC_FP32_ID ? 8 : 16; }
+
+template <class P>
+static int launch_columns(mgcu_plan* p, long b0, long b1, const typename P::T* dense, long dense_b0, typename P::T* ucols)
+{
+	typedef typename P::T T;
+	MgcuContext* c = mgcu_ctx();
+	Args<P> a;
+	memset(&a, 0, sizeof(a));
+	a.L = p->L; a.nb = p->nb; a.kt = p->kt; a.S = p->S;
+	a.W.pass = p->d_pass.as<PassRec>(); a.W.gate = p->d_gate.as<GateRec>(); a.W.npass = (int)p->ws.pass.size();
+	a.wm = p->d_mats.as<T>();
+	a.ngates = p->d.ngates;
+	if (!dense)
+	{
+		TargetProg* tp = nullptr;
+		int e = target_prog<P>(p->d.target, p->kt, tp);
+		if (e) return e;
+		a.U.pass = tp->pass.as<PassRec>(); a.U.gate = tp->gate.as<GateRec>(); a.U.npass = (int)tp->sched.pass.size();
+		a.um = tp->mats.as<T>();
+	}
+	a.dense = dense; a.dense_b0 = dense_b0;
+	a.b0 = b0; a.b1 = b1;
+	a.su = p->su.as<T>(); a.sw = p->sw.as<T>();
+	a.cache = p->cache.as<T>();
+	a.dcache = p->d.want_hess ? p->dcache.as<T>() : nullptr;
+	a.cache_per_column = p->d.want_hess ? 1 : 0;
+	a.want_grad = p->d.want_grad || p->d.want_hess;
+	a.part_f = p->part_f.as<double>();
+	a.part_g = p->part_g.as<double>();
+	a.ucols = ucols;
+	if (!a.want_grad && !ucols) a.cache = nullptr;
+	const long ncols = b1 - b0;
+	const int grid = (int)std::min<long>(p->grid_a, ncols);
+	k_columns<P><<<grid, p->threads, p->smem, c->stream>>>(a);
+	MGCU_LAUNCHED();
+	if (p->d.want_hess && !ucols)
+	{
+		a.place = p->d_place.as<int>(); a.place_w = p->d_placew.as<double>(); a.pass_of = p->d_pass_of.as<int>();
+		a.block = p->d_block.as<int>(); a.nplace = p->d.nplace; a.mdim = 8 * p->d.nblocks;
+		a.part_h = p->part_h.as<double>(); a.sh = p->sh.as<T>();
+		const long nitems = ncols * p->d.nplace * 8;
+		const int gb = (int)std::min<long>(p->grid_b, nitems);
+		k_hessian<P><<<gb, p->threads, p->smem, c->stream>>>(a, nitems);
+		MGCU_LAUNCHED();
+	}
+	return 0;
+}
+
+template <class P>
+static int set_smem_attr()
+{
+	MgcuContext* c = mgcu_ctx();
+	MGCU_TRY(cudaFuncSetAttribute(k_columns<P>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)std::min<size_t>(c->smem_optin, 227 * 1024)));
+	MGCU_TRY(cudaFuncSetAttribute(k_hessian<P>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)std::min<size_t>(c->smem_optin, 227 * 1024)));
+	return 0;
+}
+
+template <class P>
+static int occupancy(int threads, size_t smem, int& per_sm)
+{
+	int n1 = 0, n2 = 0;
+	MGCU_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n1, k_columns<P>, threads, smem));
+	MGCU_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n2, k_hessian<P>, threads, smem));
+	per_sm = std::max(1, std::min(n1, n2));
+	return 0;
+}
+
+extern "C" mgcu_plan* mgcu_plan_create(const mgcu_plan_desc* d)
+{
+	MgcuContext* c = mgcu_ctx();
+	if (!c) return nullptr;
+	if (d->L < 3 || d->L > 30)
+	{
+		mg_set_error("batched evaluation supports 3 <= nqubits <= 30 (got %d)", d->L);
+		return nullptr;
+	}
+	for (int g = 0; g < 2 * d->ngates; g++)
+		if (d->wires[g] < 0 || d->wires[g] >= d->L || (g % 2 == 1 && d->wires[g] == d->wires[g - 1]))
+		{
+			mg_set_error("invalid wire pair for gate %d", g / 2);
+			return nullptr;
+		}
+	mgcu_plan* p = new mgcu_plan();
+	p->d = *d;
+	p->wires.assign(d->wires, d->wires + 2 * d->ngates);
+	p->block.resize(std::max(d->ngates, 1));
+	for (int g = 0; g < d->ngates; g++) p->block[g] = d->block ? d->block[g] : g;
+	if (d->want_hess)
+	{
+		p->place.assign(d->place, d->place + d->nplace);
+		p->place_w.assign(d->place_w, d->place_w + (size_t)d->nplace * d->ngates);
+	}
+	p->d.wires = p->wires.data(); p->d.block = p->block.data();
+	p->d.place = p->place.data(); p->d.place_w = p->place_w.data();
+	p->L = d->L; p->nb = d->L - 1; p->S = 1L << (d->L - 1);
+	p->prec = d->precision;
+	p->tsize = prec_tsize(p->prec);
+
+	// tile size: 64 KB of state by default (2^12 complex of 16 B, 2^13 of 8 B)
+	int kt = (p->tsize == 16) ? 12 : 13;
+	const long opt_kt = mgcu_option(MG_OPT_TILE_BITS_ID);
+	if (opt_kt > 0) kt = (int)opt_kt;
+	kt = std::max(5, std::min(kt, MAXKT));   // >= 5: any gate fits beside the 3 fixed low bits
+	while (kt > 5 && ((size_t)1 << kt) * p->tsize > 200 * 1024) kt--;
+	p->kt = std::min(kt, p->nb);
+	const int Q = 1 << (p->kt - 2);
+	int threads = std::max(32, std::min(256, Q));
+	const long opt_thr = mgcu_option(MG_OPT_THREADS_ID);
+	if (opt_thr > 0) threads = (int)std::max(32L, std::min(256L, (opt_thr / 32) * 32));
+	p->threads = threads;
+	p->smem = ((size_t)1 << p->kt) * p->tsize + 2 * 128 * sizeof(unsigned) + (size_t)(threads / 32) * 16 * sizeof(double);
+
+	schedule(p->L, p->kt, p->wires.data(), d->ngates, false, p->ws);
+
+	int per_sm = 1, e = 0;
+	if (p->prec == MG_PREC_FP64_ID) { e = set_smem_attr<PrecD>(); if (!e) e = occupancy<PrecD>(threads, p->smem, per_sm); }
+	else if (p->prec == MG_PREC_FP32_ID) { e = set_smem_attr<PrecF>(); if (!e) e = occupancy<PrecF>(threads, p->smem, per_sm); }
+	else { e = set_smem_attr<PrecX>(); if (!e) e = occupancy<PrecX>(threads, p->smem, per_sm); }
+	if (e) { delete p; return nullptr; }
+	const long opt_cps = mgcu_option(MG_OPT_CTAS_PER_SM_ID);
+	if (opt_cps > 0) per_sm = (int)std::min<long>(per_sm, opt_cps);
+	long grid = (long)c->nsm * per_sm;
+	const long ncols_total = 1L << d->L;
+	const size_t col_bytes = (size_t)p->S * p->tsize;
+	const int ng = std::max(d->ngates, 1);
+	const bool grad = d->want_grad || d->want_hess;
+	// gradient caches are per block: keep them within 32 GB
+	if (grad && !d->want_hess)
+	{
+		const long cap = (long)((32ull << 30) / ((size_t)ng * col_bytes));
+		grid = std::max(1L, std::min(grid, cap));
+	}
+	grid = std::min(grid, ncols_total);
+	p->grid_a = (int)grid;
+	p->grid_b = (int)((long)c->nsm * per_sm);
+
+	// columns per chunk: Hessian caches per column (<= 16 GB) or staged target columns (<= 2 GB)
+	long chunk = ncols_total;
+	if (d->want_hess) chunk = std::max(1L, std::min(chunk, (long)((16ull << 30) / (2ull * ng * col_bytes))));
+	if (!d->target || d->target->kind == 1) chunk = std::max(1L, std::min(chunk, (long)((2ull << 30) / (col_bytes + (size_t)p->S * 16))));
+	const long opt_chunk = mgcu_option(MG_OPT_CHUNK_COLUMNS_ID);
+	if (opt_chunk > 0) chunk = std::min(chunk, opt_chunk);
+	p->chunk = chunk;
+
+	// device buffers
+	const int mdim = 8 * std::max(d->nblocks, 1);
+	e = 0;
+	if (!e) e = upload_sched(p->ws, p->d_pass, p->d_gate);
+	if (!e) e = p->su.alloc(col_bytes * grid);
+	if (!e) e = p->sw.alloc(col_bytes * grid);
+	if (!e && grad) e = p->cache.alloc(col_bytes * ng * (d->want_hess ? chunk : grid));
+	if (!e && d->want_hess) e = p->dcache.alloc(col_bytes * ng * chunk);
+	if (!e && d->want_hess) e = p->sh.alloc(col_bytes * p->grid_b);
+	if (!e) e = p->part_f.alloc(sizeof(double) * 2 * grid);
+	if (!e) e = p->part_g.alloc(sizeof(double) * 16 * ng * grid);
+	if (!e && d->want_hess) e = p->part_h.alloc(sizeof(double) * 2 * (size_t)mdim * mdim * p->grid_b);
+	if (!e) e = p->out_f.alloc(sizeof(double) * 2);
+	if (!e) e = p->out_g.alloc(sizeof(double) * 16 * ng);
+	if (!e) e = p->out_blk.alloc(sizeof(double) * 16 * std::max(d->nblocks, 1));
+	if (!e && d->want_hess) e = p->out_h.alloc(sizeof(double) * 2 * (size_t)mdim * mdim);
+	if (!e) e = p->d_block.alloc(sizeof(int) * ng);
+	if (!e) e = p->d_pass_of.alloc(sizeof(int) * ng);
+	if (!e && (!d->target || d->target->kind == 1)) e = p->cols.alloc(col_bytes * chunk);
+	if (!e && !d->target) e = p->cols64.alloc((size_t)p->S * 16 * chunk);
+	if (!e && d->want_hess) e = p->d_place.alloc(sizeof(int) * std::max(d->nplace, 1));
+	if (!e && d->want_hess) e = p->d_placew.alloc(sizeof(double) * std::max<size_t>((size_t)d->nplace * ng, 1));
+	if (e) { delete p; return nullptr; }
+	cudaStream_t st = c->stream;
+	bool ok = cudaMemcpyAsync(p->d_block.p, p->block.data(), sizeof(int) * ng, cudaMemcpyHostToDevice, st) == cudaSuccess;
+	ok = ok && cudaMemcpyAsync(p->d_pass_of.p, p->ws.pass_of.data(), sizeof(int) * d->ngates, cudaMemcpyHostToDevice, st) == cudaSuccess;
+	if (d->want_hess)
+	{
+		ok = ok && cudaMemcpyAsync(p->d_place.p, p->place.data(), sizeof(int) * d->nplace, cudaMemcpyHostToDevice, st) == cudaSuccess;
+		ok = ok && cudaMemcpyAsync(p->d_placew.p, p->place_w.data(), sizeof(double) * p->place_w.size(), cudaMemcpyHostToDevice, st) == cudaSuccess;
+	}
+	ok = ok && cudaStreamSynchronize(st) == cudaSuccess;
+	if (!ok) { mg_set_error("uploading an evaluation plan failed"); delete p; return nullptr; }
+	return p;
+}
+
+extern "C" void mgcu_plan_destroy(mgcu_plan* p) { delete p; }
+
+extern "C" long mgcu_plan_chunk_columns(const mgcu_plan* p) { return p->chunk; }
+
+extern "C" int mgcu_plan_set_gates(mgcu_plan* p, const mgg* gates)
+{
+	if (p->prec == MG_PREC_FP64_ID) return upload_mats<PrecD>(gates, p->d.ngates, p->d_mats);
+	if (p->prec == MG_PREC_FP32_ID) return upload_mats<PrecF>(gates, p->d.ngates, p->d_mats);
+	return upload_mats<PrecX>(gates, p->d.ngates, p->d_mats);
+}
+
+extern "C" int mgcu_plan_begin(mgcu_plan* p)
+{
+	cudaStream_t st = mgcu_ctx()->stream;
+	MGCU_TRY(cudaMemsetAsync(p->part_f.p, 0, p->part_f.n, st));
+	MGCU_TRY(cudaMemsetAsync(p->part_g.p, 0, p->part_g.n, st));
+	if (p->d.want_hess) MGCU_TRY(cudaMemsetAsync(p->part_h.p, 0, p->part_h.n, st));
+	return 0;
+}
+
+template <class P>
+static int plan_columns_t(mgcu_plan* p, long b0, long b1, const mgc* host_cols)
+{
+	typedef typename P::T T;
+	MgcuContext* c = mgcu_ctx();
+	mgcu_target* t = p->d.target;
+	for (long c0 = b0; c0 < b1; c0 += p->chunk)
+	{
+		const long c1 = std::min(b1, c0 + p->chunk);
+		const long n = (c1 - c0) * p->S;
+		const T* dense = nullptr;
+		long dense_b0 = c0;
+		if (!t)
+		{
+			MGCU_TRY(cudaMemcpyAsync(p->cols64.p, host_cols + (size_t)(c0 - b0) * p->S, sizeof(double2) * n, cudaMemcpyHostToDevice, c->stream));
+			k_convert<P><<<grid_cap(n, 256), 256, 0, c->stream>>>(p->cols64.as<double2>(), n, p->cols.as<T>());
+			MGCU_LAUNCHED();
+			dense = p->cols.as<T>();
+		}
+		else if (t->kind == 1)
+		{
+			k_dense_columns<P><<<grid_cap(n, 256), 256, 0, c->stream>>>(t->dense.as<double2>(), p->L, c0, c1, p->cols.as<T>());
+			MGCU_LAUNCHED();
+			dense = p->cols.as<T>();
+		}
+		else if (t->resident)
+		{
+			const int id = P::kId;
+			if (!t->res_valid[id] || t->res_kt[id] != p->kt)
+			{
+				const long N = 1L << p->L;
+				int e = t->res_cols[id].alloc((size_t)N * p->S * sizeof(T));
+				if (e) return e;
+				e = launch_columns<P>(p, 0, N, nullptr, 0, t->res_cols[id].as<T>());
+				if (e) return e;
+				t->res_valid[id] = true; t->res_kt[id] = p->kt;
+			}
+			dense = t->res_cols[id].as<T>();
+			dense_b0 = 0;
+		}
+		int e = launch_columns<P>(p, c0, c1, dense, dense_b0, nullptr);
+		if (e) return e;
+	}
+	return 0;
+}
+
+extern "C" int mgcu_plan_columns(mgcu_plan* p, long b0, long b1, const mgc* host_cols)
+{
+	if (b1 <= b0) return 0;
+	if (p->prec == MG_PREC_FP64_ID) return plan_columns_t<PrecD>(p, b0, b1, host_cols);
+	if (p->prec == MG_PREC_FP32_ID) return plan_columns_t<PrecF>(p, b0, b1, host_cols);
+	return plan_columns_t<PrecX>(p, b0, b1, host_cols);
+}
+
+extern "C" int mgcu_plan_finish(mgcu_plan* p)
+{
+	MgcuContext* c = mgcu_ctx();
+	cudaStream_t st = c->stream;
+	const int ng = std::max(p->d.ngates, 1);
+	k_sum_parts<<<1, 32, 0, st>>>(p->part_f.as<double>(), p->grid_a, 2, p->out_f.as<double>());
+	MGCU_LAUNCHED();
+	if (p->d.want_grad || p->d.want_hess)
+	{
+		k_sum_parts<<<grid_cap(16L * ng, 128), 128, 0, st>>>(p->part_g.as<double>(), p->grid_a, 16L * ng, p->out_g.as<double>());
+		MGCU_LAUNCHED();
+		k_block_sum<<<(16 * p->d.nblocks + 127) / 128, 128, 0, st>>>(p->out_g.as<double>(), p->d_block.as<int>(), p->d.ngates, p->d.nblocks, p->out_blk.as<double>());
+		MGCU_LAUNCHED();
+	}
+	if (p->d.want_hess)
+	{
+		const long mdim = 8L * p->d.nblocks;
+		k_sum_parts<<<grid_cap(2 * mdim * mdim, 128), 128, 0, st>>>(p->part_h.as<double>(), p->grid_b, 2 * mdim * mdim, p->out_h.as<double>());
+		MGCU_LAUNCHED();
+		k_symm_diag<<<grid_cap(mdim * mdim, 256), 256, 0, st>>>(p->d.nblocks, p->out_h.as<double2>());
+		MGCU_LAUNCHED();
+		k_mirror<<<grid_cap(mdim * mdim, 256), 256, 0, st>>>(p->d.nblocks, p->out_h.as<double2>());
+		MGCU_LAUNCHED();
+	}
+	return 0;
+}
+
+extern "C" int mgcu_plan_fetch(mgcu_plan* p, mgc* f, mgg* dblocks, mgc* hess)
+{
+	cudaStream_t st = mgcu_ctx()->stream;
+	if (f) MGCU_TRY(cudaMemcpyAsync(f, p->out_f.p, sizeof(double) * 2, cudaMemcpyDeviceToHost, st));
+	if (dblocks && (p->d.want_grad || p->d.want_hess))
+		MGCU_TRY(cudaMemcpyAsync(dblocks, p->out_blk.p, sizeof(double) * 16 * p->d.nblocks, cudaMemcpyDeviceToHost, st));
+	if (hess && p->d.want_hess)
+		MGCU_TRY(cudaMemcpyAsync(hess, p->out_h.p, sizeof(double) * 2 * 64 * (size_t)p->d.nblocks * p->d.nblocks, cudaMemcpyDeviceToHost, st));
+	MGCU_TRY(cudaStreamSynchronize(st));
+	return 0;
+}
+
+// projection of gradient and Hessian on the GPU (mgcu_algebra.cu)
+extern int mgcu_project_dev(const mgg* vblocks_host, int nblocks, const double* dgrad_dev, const double* hess_dev,
+	double* grad_vec, double* H);
+
+extern "C" int mgcu_plan_project(mgcu_plan* p, const mgg* vblocks, double* grad_vec, double* H)
+{
+	return mgcu_project_dev(vblocks, p->d.nblocks, p->out_blk.as<double>(), p->d.want_hess ? p->out_h.as<double>() : nullptr, grad_vec, H);
+}
+
+extern "C" double mgcu_plan_time_ms(mgcu_plan* p, long b0, long b1, int steps, int flush_l2)
+{
+	MgcuContext* c = mgcu_ctx();
+	if (flush_l2 && p->flush.alloc(512ull << 20)) return -1;
+	double total = 0;
+	for (int s = 0; s < steps; s++)
+	{
+		if (flush_l2 && cudaMemsetAsync(p->flush.p, s & 0xff, p->flush.n, c->stream) != cudaSuccess) return -1;
+		cudaEventRecord(c->ev0, c->stream);
+		if (mgcu_plan_begin(p) || mgcu_plan_columns(p, b0, b1, nullptr) || mgcu_plan_finish(p)) return -1;
+		cudaEventRecord(c->ev1, c->stream);
+		if (cudaEventSynchronize(c->ev1) != cudaSuccess) return -1;
+		float ms = 0;
+		cudaEventElapsedTime(&ms, c->ev0, c->ev1);
+		total += ms;
+	}
+	return total;
+}

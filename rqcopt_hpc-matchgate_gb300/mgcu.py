@@ -1,0 +1,432 @@
+"""ctypes binding of the matchgate C API (the reference's matchgate_brickwall.h,
+matchgate_target.h, trust_region.h, gate.h, quantum_circuit.h, matchgate.h) and of
+this library's extensions (mg_gb300.h).
+
+``MatchgateLib(path)`` binds any shared library exporting that C API: this project's
+``_build/libmgcu.so``, or a build of the reference, so both can be driven through the
+same C entry points with numpy arrays.  Conventions:
+
+* a gate is a complex128 array of 8 entries (center block row-major, then corner
+  block), i.e. the memory of ``struct matchgate``; lists of gates are (n, 8) arrays;
+* perms are int32 arrays (nlayers, L); wires are int32 arrays (ngates, 2);
+* a target map is a pair (ufunc, udata) of addresses: ``lib.target_*`` returns a
+  GPU target of this library, ``ufunc_address(cfunc)`` wraps C or Python callbacks.
+"""
+import ctypes as C
+import os
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+DEFAULT_LIB = os.path.join(HERE, "_build", "libmgcu.so")
+
+PREC_FP64, PREC_MIXED, PREC_FP32 = 0, 1, 2
+OPT_TILE_BITS, OPT_THREADS, OPT_CHUNK_COLUMNS, OPT_CTAS_PER_SM = 1, 2, 3, 4
+EVAL_TARGET, EVAL_GRADIENT, EVAL_HESSIAN, EVAL_TI = 0, 1, 2, 4
+
+P = C.c_void_p
+cd = np.complex128
+
+
+class StateVector(C.Structure):
+    _fields_ = [("data", C.c_void_p), ("nqubits", C.c_int)]
+
+
+class StateVectorArray(C.Structure):
+    _fields_ = [("data", C.c_void_p), ("nqubits", C.c_int), ("nstates", C.c_int)]
+
+
+class CircuitCache(C.Structure):
+    _fields_ = [("psi_list", C.POINTER(StateVector)), ("nqubits", C.c_int), ("ngates", C.c_int)]
+
+
+class TcgParams(C.Structure):
+    _fields_ = [("maxiter", C.c_int), ("abstol", C.c_double), ("reltol", C.c_double)]
+
+
+TargetFunc = C.CFUNCTYPE(C.c_double, C.POINTER(C.c_double), C.c_void_p, C.POINTER(C.c_double))
+TargetGradHessFunc = C.CFUNCTYPE(C.c_double, C.POINTER(C.c_double), C.c_void_p, C.POINTER(C.c_double),
+                                 C.POINTER(C.c_double), C.POINTER(C.c_double))
+RetractFunc = C.CFUNCTYPE(None, C.POINTER(C.c_double), C.POINTER(C.c_double), C.c_void_p, C.POINTER(C.c_double))
+LinearFunc = C.CFUNCTYPE(C.c_int, C.POINTER(StateVector), C.c_void_p, C.POINTER(StateVector))
+
+
+class RtrParams(C.Structure):
+    _fields_ = [("tcg_params", TcgParams), ("rho_trust", C.c_double), ("radius_init", C.c_double),
+                ("maxradius", C.c_double), ("g_func", C.c_void_p), ("g_data", C.c_void_p), ("g_iter", C.c_void_p)]
+
+
+def _p(a):
+    return a.ctypes.data_as(P) if a is not None else None
+
+
+def gates_arr(g):
+    return np.ascontiguousarray(np.asarray(g, dtype=cd).reshape(-1, 8))
+
+
+def _sv(a, L):
+    return StateVector(a.ctypes.data, L)
+
+
+def _perm_ptrs(perms, L):
+    rows = [np.ascontiguousarray(np.asarray(p, dtype=np.int32).reshape(L)) for p in perms]
+    arr = (C.c_void_p * max(len(rows), 1))(*[r.ctypes.data for r in rows])
+    return arr, rows
+
+
+def ufunc_address(f):
+    """Address of a linear_func: a ctypes function of a loaded library or a LinearFunc."""
+    return C.cast(f, C.c_void_p).value
+
+
+def python_ufunc(fn):
+    """Wrap fn(psi: np.ndarray) -> np.ndarray as a LinearFunc (keep the result alive)."""
+    def cb(psi_p, udata, out_p):
+        L = psi_p.contents.nqubits
+        n = 1 << L
+        psi = np.ctypeslib.as_array(C.cast(psi_p.contents.data, C.POINTER(C.c_double)), shape=(2 * n,)).view(cd)
+        out = np.ctypeslib.as_array(C.cast(out_p.contents.data, C.POINTER(C.c_double)), shape=(2 * n,)).view(cd)
+        out[:] = fn(psi.copy())
+        return 0
+    return LinearFunc(cb)
+
+
+class MatchgateLib:
+    """numpy-facing binding of the matchgate C API exported by ``path``."""
+
+    def __init__(self, path=DEFAULT_LIB):
+        self.path = path
+        self.lib = C.CDLL(path)
+        L = self.lib
+        self.is_gb300 = hasattr(L, "mg_set_precision")
+        if self.is_gb300:
+            for name in ["mg_target_brickwall", "mg_target_circuit", "mg_target_dense", "mg_plan_brickwall"]:
+                getattr(L, name).restype = P
+            L.mg_target_brickwall.argtypes = [P, C.c_int, P, C.c_int]
+            L.mg_target_circuit.argtypes = [P, C.c_int, P, C.c_int]
+            L.mg_target_dense.argtypes = [P, C.c_int]
+            L.mg_target_free.argtypes = [P]
+            L.mg_target_set_resident.argtypes = [P, C.c_int]
+            L.mg_last_error.restype = C.c_char_p
+            L.mg_plan_brickwall.argtypes = [P, P, P, C.c_int, C.c_int, P, C.c_int]
+            L.mg_plan_set_gates.argtypes = [P, P]
+            L.mg_plan_run.argtypes = [P]
+            L.mg_plan_results.argtypes = [P, P, P, P, P, P]
+            L.mg_plan_free.argtypes = [P]
+            L.mg_plan_time_ms.argtypes = [P, C.c_int, C.c_int]
+            L.mg_plan_time_ms.restype = C.c_double
+            L.mg_launch_count.restype = C.c_long
+            L.mg_get_option.restype = C.c_long
+            L.mg_set_option.argtypes = [C.c_int, C.c_long]
+            L.mg_measure_fp32_peak_gflops.restype = C.c_double
+            L.mg_measure_fp64_peak_gflops.restype = C.c_double
+            L.mg_brickwall_target_and_gradient_columns.argtypes = [P, P, P, C.c_int, C.c_int, P, C.c_long, C.c_long, P, P]
+        L.truncated_cg_hmat.restype = C.c_bool
+        L.truncated_cg_hmat.argtypes = [P, P, C.c_int, C.c_double, C.POINTER(TcgParams), P]
+        for name in ["uniform_distance", "uniform_distance_real"]:
+            getattr(L, name).restype = C.c_double
+        self.mg_target_apply = ufunc_address(L.mg_target_apply) if self.is_gb300 else None
+        self._keep = []
+
+    # ------------------------------------------------------------------ settings
+    def set_precision(self, p):
+        return self.lib.mg_set_precision(p)
+
+    def set_option(self, opt, value):
+        return self.lib.mg_set_option(opt, value)
+
+    def last_error(self):
+        return self.lib.mg_last_error().decode()
+
+    def launch_count(self):
+        return self.lib.mg_launch_count()
+
+    # ------------------------------------------------------------------ GPU targets
+    def target_brickwall(self, ulist, uperms, L):
+        ul = gates_arr(ulist)
+        pp, rows = _perm_ptrs(uperms, L)
+        h = self.lib.mg_target_brickwall(_p(ul), len(ul), C.cast(pp, P), L)
+        if not h:
+            raise RuntimeError("mg_target_brickwall failed: " + self.last_error())
+        return h
+
+    def target_circuit(self, gates, wires, L):
+        g = gates_arr(gates)
+        w = np.ascontiguousarray(np.asarray(wires, np.int32).reshape(-1))
+        h = self.lib.mg_target_circuit(_p(g), len(g), _p(w), L)
+        if not h:
+            raise RuntimeError("mg_target_circuit failed: " + self.last_error())
+        return h
+
+    def target_dense(self, U, L):
+        U = np.ascontiguousarray(U, dtype=cd)
+        h = self.lib.mg_target_dense(_p(U), L)
+        if not h:
+            raise RuntimeError("mg_target_dense failed: " + self.last_error())
+        return h
+
+    def target_free(self, h):
+        self.lib.mg_target_free(h)
+
+    # ------------------------------------------------------------------ single gates (gate.h)
+    def apply_matchgate(self, g, i, j, psi):
+        g = gates_arr(g); psi = np.ascontiguousarray(psi, dtype=cd); L = int(np.log2(len(psi)))
+        out = np.zeros_like(psi)
+        a, b = _sv(psi, L), _sv(out, L)
+        self.lib.apply_matchgate(_p(g), i, j, C.byref(a), C.byref(b))
+        return out
+
+    def apply_matchgate_backward(self, g, i, j, psi, dpsi_out):
+        g = gates_arr(g); psi = np.ascontiguousarray(psi, dtype=cd); d = np.ascontiguousarray(dpsi_out, dtype=cd)
+        L = int(np.log2(len(psi))); dpsi = np.zeros_like(psi); dg = np.zeros((1, 8), cd)
+        self.lib.apply_matchgate_backward(_p(g), i, j, C.byref(_sv(psi, L)), C.byref(_sv(d, L)), C.byref(_sv(dpsi, L)), _p(dg))
+        return dpsi, dg[0]
+
+    def apply_matchgate_to_array(self, g, i, j, arr):
+        g = gates_arr(g); a = np.ascontiguousarray(arr, dtype=cd); L = int(np.log2(a.shape[0])); out = np.zeros_like(a)
+        x = StateVectorArray(a.ctypes.data, L, a.shape[1]); y = StateVectorArray(out.ctypes.data, L, a.shape[1])
+        self.lib.apply_matchgate_to_array(_p(g), i, j, C.byref(x), C.byref(y))
+        return out
+
+    def apply_matchgate_backward_array(self, g, i, j, arr, dpsi_out):
+        g = gates_arr(g); a = np.ascontiguousarray(arr, dtype=cd); d = np.ascontiguousarray(dpsi_out, dtype=cd)
+        L = int(np.log2(a.shape[0])); dgs = np.zeros((a.shape[1], 8), cd)
+        x = StateVectorArray(a.ctypes.data, L, a.shape[1])
+        self.lib.apply_matchgate_backward_array(_p(g), i, j, C.byref(x), C.byref(_sv(d, L)), _p(dgs))
+        return dgs
+
+    def apply_placeholder(self, i, j, psi, nout=8):
+        psi = np.ascontiguousarray(psi, dtype=cd); L = int(np.log2(len(psi))); out = np.zeros((len(psi), nout), cd)
+        y = StateVectorArray(out.ctypes.data, L, nout)
+        fn = self.lib.apply_matchgate_placeholder if nout == 8 else self.lib.apply_gate_placeholder
+        fn(i, j, C.byref(_sv(psi, L)), C.byref(y))
+        return out
+
+    # ------------------------------------------------------------------ sweeps on one vector
+    def _cache(self, L, ng, data=None):
+        rows = np.zeros((ng, 1 << L), cd) if data is None else np.ascontiguousarray(data, dtype=cd)
+        svs = (StateVector * ng)(*[StateVector(rows[k].ctypes.data, L) for k in range(ng)])
+        cache = CircuitCache(C.cast(svs, C.POINTER(StateVector)), L, ng)
+        return cache, rows, svs
+
+    def brickwall_apply(self, vlist, perms, psi):
+        v = gates_arr(vlist); psi = np.ascontiguousarray(psi, dtype=cd); L = int(np.log2(len(psi)))
+        pp, rows = _perm_ptrs(perms, L); out = np.zeros_like(psi)
+        r = self.lib.apply_matchgate_brickwall_unitary(_p(v), len(v), C.cast(pp, P), C.byref(_sv(psi, L)), C.byref(_sv(out, L)))
+        assert r == 0
+        return out
+
+    def brickwall_forward(self, vlist, perms, psi):
+        v = gates_arr(vlist); psi = np.ascontiguousarray(psi, dtype=cd); L = int(np.log2(len(psi)))
+        pp, rows = _perm_ptrs(perms, L); out = np.zeros_like(psi)
+        cache, crow, svs = self._cache(L, len(v) * (L // 2))
+        r = self.lib.matchgate_brickwall_unitary_forward(_p(v), len(v), C.cast(pp, P), C.byref(_sv(psi, L)), C.byref(cache), C.byref(_sv(out, L)))
+        assert r == 0
+        return out, crow
+
+    def brickwall_backward(self, vlist, perms, cache_rows, dpsi_out, hessian=False, ti=False):
+        v = gates_arr(vlist); d = np.ascontiguousarray(dpsi_out, dtype=cd); L = int(np.log2(len(d)))
+        pp, rows = _perm_ptrs(perms, L); dpsi = np.zeros_like(d); dv = np.zeros((len(v), 8), cd)
+        cache, crow, svs = self._cache(L, len(v) * (L // 2), cache_rows)
+        if not hessian:
+            r = self.lib.matchgate_brickwall_unitary_backward(_p(v), len(v), C.cast(pp, P), C.byref(cache), C.byref(_sv(d, L)),
+                                                             C.byref(_sv(dpsi, L)), _p(dv))
+            assert r == 0
+            return dpsi, dv
+        m = 8 * len(v); hess = np.zeros((m, m), cd)
+        fn = self.lib.matchgate_ti_brickwall_unitary_backward_hessian if ti else self.lib.matchgate_brickwall_unitary_backward_hessian
+        r = fn(_p(v), len(v), C.cast(pp, P), C.byref(cache), C.byref(_sv(d, L)), C.byref(_sv(dpsi, L)), _p(dv), _p(hess))
+        assert r == 0
+        return dpsi, dv, hess
+
+    def circuit_apply(self, gates, wires, psi):
+        g = gates_arr(gates); w = np.ascontiguousarray(np.asarray(wires, np.int32).reshape(-1))
+        psi = np.ascontiguousarray(psi, dtype=cd); L = int(np.log2(len(psi))); out = np.zeros_like(psi)
+        r = self.lib.apply_quantum_matchgate_circuit(_p(g), len(g), _p(w), C.byref(_sv(psi, L)), C.byref(_sv(out, L)))
+        assert r == 0
+        return out
+
+    def circuit_forward(self, gates, wires, psi):
+        g = gates_arr(gates); w = np.ascontiguousarray(np.asarray(wires, np.int32).reshape(-1))
+        psi = np.ascontiguousarray(psi, dtype=cd); L = int(np.log2(len(psi))); out = np.zeros_like(psi)
+        cache, crow, svs = self._cache(L, len(g))
+        r = self.lib.quantum_matchgate_circuit_forward(_p(g), len(g), _p(w), C.byref(_sv(psi, L)), C.byref(cache), C.byref(_sv(out, L)))
+        assert r == 0
+        return out, crow
+
+    def circuit_backward(self, gates, wires, cache_rows, dpsi_out):
+        g = gates_arr(gates); w = np.ascontiguousarray(np.asarray(wires, np.int32).reshape(-1))
+        d = np.ascontiguousarray(dpsi_out, dtype=cd); L = int(np.log2(len(d))); dpsi = np.zeros_like(d); dg = np.zeros((len(g), 8), cd)
+        cache, crow, svs = self._cache(L, len(g), cache_rows)
+        r = self.lib.quantum_matchgate_circuit_backward(_p(g), len(g), _p(w), C.byref(cache), C.byref(_sv(d, L)), C.byref(_sv(dpsi, L)), _p(dg))
+        assert r == 0
+        return dpsi, dg
+
+    # ------------------------------------------------------------------ traces (matchgate_target.h)
+    def circuit_target(self, ufunc, udata, gates, wires, L):
+        g = gates_arr(gates); w = np.ascontiguousarray(np.asarray(wires, np.int32).reshape(-1)); f = np.zeros(1, cd)
+        rc = self.lib.matchgate_circuit_unitary_target(P(ufunc), P(udata), _p(g), len(g), _p(w), L, _p(f))
+        return rc, f[0]
+
+    def circuit_target_and_gradient(self, ufunc, udata, gates, wires, L):
+        g = gates_arr(gates); w = np.ascontiguousarray(np.asarray(wires, np.int32).reshape(-1))
+        f = np.zeros(1, cd); dg = np.zeros((len(g), 8), cd)
+        rc = self.lib.matchgate_circuit_unitary_target_and_gradient(P(ufunc), P(udata), _p(g), len(g), _p(w), L, _p(f), _p(dg))
+        return rc, f[0], dg
+
+    def circuit_target_gradient_hessian(self, ufunc, udata, gates, wires, L):
+        g = gates_arr(gates); w = np.ascontiguousarray(np.asarray(wires, np.int32).reshape(-1))
+        f = np.zeros(1, cd); dg = np.zeros((len(g), 8), cd); m = 8 * len(g); h = np.zeros((m, m), cd)
+        rc = self.lib.matchgate_circuit_unitary_target_gradient_hessian(P(ufunc), P(udata), _p(g), len(g), _p(w), L, _p(f), _p(dg), _p(h))
+        return rc, f[0], dg, h
+
+    def brickwall_target(self, ufunc, udata, vlist, perms, L):
+        v = gates_arr(vlist); pp, rows = _perm_ptrs(perms, L); f = np.zeros(1, cd)
+        rc = self.lib.matchgate_brickwall_unitary_target(P(ufunc), P(udata), _p(v), len(v), L, C.cast(pp, P), _p(f))
+        return rc, f[0]
+
+    def brickwall_target_and_gradient(self, ufunc, udata, vlist, perms, L):
+        v = gates_arr(vlist); pp, rows = _perm_ptrs(perms, L); f = np.zeros(1, cd); dv = np.zeros((len(v), 8), cd)
+        rc = self.lib.matchgate_brickwall_unitary_target_and_gradient(P(ufunc), P(udata), _p(v), len(v), L, C.cast(pp, P), _p(f), _p(dv))
+        return rc, f[0], dv
+
+    def brickwall_target_gradient_hessian(self, ufunc, udata, vlist, perms, L, ti=False, parallel=False):
+        v = gates_arr(vlist); pp, rows = _perm_ptrs(perms, L); f = np.zeros(1, cd); dv = np.zeros((len(v), 8), cd)
+        m = 8 * len(v); h = np.zeros((m, m), cd)
+        if ti:
+            fn = self.lib.matchgate_ti_brickwall_unitary_target_gradient_hessian
+        elif parallel:
+            fn = self.lib.parallel_matchgate_brickwall_unitary_target_gradient_hessian
+        else:
+            fn = self.lib.matchgate_brickwall_unitary_target_gradient_hessian
+        rc = fn(P(ufunc), P(udata), _p(v), len(v), L, C.cast(pp, P), _p(f), _p(dv), _p(h))
+        return rc, f[0], dv, h
+
+    def brickwall_gradvec_hessmat(self, ufunc, udata, vlist, perms, L):
+        v = gates_arr(vlist); pp, rows = _perm_ptrs(perms, L); f = np.zeros(1, cd)
+        m = 8 * len(v); g = np.zeros(m); H = np.zeros((m, m))
+        rc = self.lib.matchgate_brickwall_unitary_target_gradient_vector_hessian_matrix(P(ufunc), P(udata), _p(v), len(v), L, C.cast(pp, P),
+                                                                                       _p(f), _p(g), _p(H))
+        return rc, f[0], g, H
+
+    def brickwall_projected_gradient(self, ufunc, udata, vlist, perms, L):
+        v = gates_arr(vlist); pp, rows = _perm_ptrs(perms, L); f = np.zeros(1, cd); g = np.zeros(8 * len(v))
+        rc = self.lib.matchgate_brickwall_unitary_target_and_projected_gradient(P(ufunc), P(udata), _p(v), len(v), L, C.cast(pp, P), _p(f), _p(g))
+        return rc, f[0], g
+
+    def brickwall_columns(self, ufunc, udata, vlist, perms, L, b0, b1, gradient=True):
+        v = gates_arr(vlist); pp, rows = _perm_ptrs(perms, L); f = np.zeros(1, cd); dv = np.zeros((len(v), 8), cd)
+        rc = self.lib.mg_brickwall_target_and_gradient_columns(P(ufunc), P(udata), _p(v), len(v), L, C.cast(pp, P), b0, b1, _p(f),
+                                                               _p(dv) if gradient else None)
+        return rc, f[0], dv
+
+    # ------------------------------------------------------------------ device-resident plans
+    def plan_brickwall(self, ufunc, udata, vlist, perms, L, what):
+        v = gates_arr(vlist); pp, rows = _perm_ptrs(perms, L)
+        h = self.lib.mg_plan_brickwall(P(ufunc), P(udata), _p(v), len(v), L, C.cast(pp, P), what)
+        if not h:
+            raise RuntimeError("mg_plan_brickwall failed: " + self.last_error())
+        return h
+
+    def plan_results(self, plan, nlayers, grad=False, hess=False, proj=False):
+        f = np.zeros(1, cd)
+        dv = np.zeros((nlayers, 8), cd) if grad else None
+        m = 8 * nlayers
+        h = np.zeros((m, m), cd) if hess else None
+        g = np.zeros(m) if proj else None
+        H = np.zeros((m, m)) if (proj and hess) else None
+        rc = self.lib.mg_plan_results(P(plan), _p(f), _p(dv), _p(h), _p(g), _p(H))
+        assert rc == 0, self.last_error()
+        return f[0], dv, h, g, H
+
+    # ------------------------------------------------------------------ algebra (matchgate.h)
+    def _mg(self, name, *gs):
+        gs = [gates_arr(g) for g in gs]
+        out = np.zeros((1, 8), cd)
+        getattr(self.lib, name)(*[_p(g) for g in gs], _p(out))
+        return out[0]
+
+    def multiply(self, a, b):
+        return self._mg("multiply_matchgates", a, b)
+
+    def project_tangent(self, u, z):
+        return self._mg("project_tangent_matchgate", u, z)
+
+    def polar(self, a):
+        return self._mg("polar_matchgate_factor", a)
+
+    def real_to_tangent(self, r, v):
+        r = np.ascontiguousarray(r, np.float64); v = gates_arr(v); out = np.zeros((1, 8), cd)
+        self.lib.real_to_tangent_matchgate(_p(r), _p(v), _p(out))
+        return out[0]
+
+    def tangent_to_real(self, v, z):
+        v = gates_arr(v); z = gates_arr(z); r = np.zeros(8)
+        self.lib.tangent_matchgate_to_real(_p(v), _p(z), _p(r))
+        return r
+
+    def retract(self, u, eta):
+        u = gates_arr(u); eta = np.ascontiguousarray(eta, np.float64); out = np.zeros((1, 8), cd)
+        self.lib.retract_matchgate(_p(u), _p(eta), _p(out))
+        return out[0]
+
+    def truncated_cg(self, grad, hess, radius, maxiter, abstol=1e-8, reltol=1e-6):
+        g = np.ascontiguousarray(grad, np.float64); h = np.ascontiguousarray(hess, np.float64); z = np.zeros_like(g)
+        prm = TcgParams(maxiter, abstol, reltol)
+        onb = self.lib.truncated_cg_hmat(_p(g), _p(h), len(g), radius, C.byref(prm), _p(z))
+        return z, bool(onb)
+
+    # ------------------------------------------------------------------ trust region
+    def optimize_brickwall(self, ufunc, udata, vlist0, perms, L, niter, tcg_maxiter=None,
+                           rho_trust=0.125, radius_init=0.01, maxradius=0.1):
+        """riemannian_trust_region_optimize_hmat driven like the reference's
+        optimize_matchgate_brickwall_circuit_hmat (src/mg_brickwall_opt.c:99-122):
+        f and f_deriv_hess call this library's evaluations, retraction per layer."""
+        v0 = gates_arr(vlist0); nl = len(v0); n = 8 * nl; m = 16 * nl
+        pp, rows = _perm_ptrs(perms, L)
+        lib = self.lib
+
+        def f_cb(x, fdata, fc):
+            fv = np.zeros(1, cd)
+            rc = lib.matchgate_brickwall_unitary_target(P(ufunc), P(udata), C.cast(x, P), nl, L, C.cast(pp, P), _p(fv))
+            if rc < 0:
+                return -1.0
+            fc[0] = fv[0].real; fc[1] = fv[0].imag
+            return fv[0].real
+
+        def fdh_cb(x, fdata, fc, grad, hess):
+            fv = np.zeros(1, cd)
+            rc = lib.matchgate_brickwall_unitary_target_gradient_vector_hessian_matrix(
+                P(ufunc), P(udata), C.cast(x, P), nl, L, C.cast(pp, P), _p(fv), C.cast(grad, P), C.cast(hess, P))
+            if rc < 0:
+                return -1.0
+            fc[0] = fv[0].real; fc[1] = fv[0].imag
+            return fv[0].real
+
+        def retract_cb(x, eta, rdata, xs):
+            ax, ae, axs = (C.cast(q, C.c_void_p).value for q in (x, eta, xs))
+            for i in range(nl):   # one gate = 16 doubles, one tangent vector = 8 doubles
+                lib.retract_matchgate(P(ax + 128 * i), P(ae + 64 * i), P(axs + 128 * i))
+
+        fcb, fdhcb, rcb = TargetFunc(f_cb), TargetGradHessFunc(fdh_cb), RetractFunc(retract_cb)
+        prm = RtrParams()
+        prm.tcg_params = TcgParams(tcg_maxiter if tcg_maxiter is not None else 2 * 16 * nl, 1e-8, 1e-6)
+        prm.rho_trust, prm.radius_init, prm.maxradius = rho_trust, radius_init, maxradius
+        f_iter = np.zeros(niter + 1); f_citer = np.zeros(niter + 1, cd); xf = np.zeros((nl, 8), cd)
+        lib.riemannian_trust_region_optimize_hmat(fcb, fdhcb, None, rcb, None, n, _p(v0), m, C.byref(prm), niter,
+                                                  _p(f_iter), _p(f_citer), _p(xf))
+        return f_iter, f_citer, xf
+
+
+_default = None
+
+
+def default_lib():
+    """The in-tree libmgcu.so (raises if it has not been built)."""
+    global _default
+    if _default is None:
+        if not os.path.exists(DEFAULT_LIB):
+            raise RuntimeError("libmgcu.so is missing: build it with rqcopt_hpc-matchgate_gb300/build.py "
+                               "(this library has no CPU implementation to fall back to)")
+        _default = MatchgateLib(DEFAULT_LIB)
+    return _default
