@@ -1,0 +1,298 @@
+#!/usr/bin/env python
+"""Benchmark: gradient evaluations per second of the matchgate-brickwall fit at L=16.
+
+Workload (seeded, synthetic): the spinful 1-D Fermi-Hubbard model on 8 sites x 2 spins
+(interleaved, Jordan-Wigner, open chain), J=1, U=4, total time t=0.25, as a
+second-order Trotter circuit of 64 steps built from matchgates (3336 gates); the fitted
+circuit is a 5-layer periodic brickwall initialised at identity plus 1e-2 seeded noise.
+One step = one gradient evaluation: f = -tr(U^dagger W) and the gate gradients, traced
+over all 2^16 basis columns, target applied per column (nothing cached between steps).
+
+The timed arm (default) runs the float-float ("mixed") engine; the FP64 engine is timed on
+a column sample beside it and the mixed result's relative error against FP64 is reported.
+--impl reference times the oracle port (the reference's CPU algorithm restated in C,
+OpenMP over basis columns) on the host's cores on a bounded column sample.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gb300|reference]
+"""
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+PKG = os.path.join(ROOT, "rqcopt_hpc-matchgate_gb300")
+for _p in (PKG, os.path.join(ROOT, "oracle")):
+    if _p not in sys.path:
+        sys.path.insert(0, _p)
+
+METRIC = "grad evals/s at L=16 (mixed vs FP64 GPU, rel err<=1e-9); serving p50/p99 ms"
+UNIT = "grad evals/s"
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=3)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--L", type=int, default=16)
+    ap.add_argument("--layers", type=int, default=5)
+    ap.add_argument("--trotter-steps", type=int, default=64)
+    ap.add_argument("--precision", default="mixed", choices=["mixed", "fp64", "fp32"])
+    ap.add_argument("--fp64-columns", type=int, default=2048, help="column sample for the FP64 comparison")
+    ap.add_argument("--cpu-seconds", type=float, default=15.0, help="budget of the CPU baseline sample")
+    ap.add_argument("--no-cpu", action="store_true")
+    return ap.parse_args()
+
+
+def dist_env():
+    return int(os.environ.get("RANK", 0)), int(os.environ.get("WORLD_SIZE", 1)), int(os.environ.get("LOCAL_RANK", 0))
+
+
+class Dist:
+    """barrier / max over ranks on the host (gloo); no data-path collective: replicas"""
+
+    def __init__(self, world):
+        self.world = world
+        if world > 1:
+            import torch.distributed as td
+            os.environ.setdefault("MASTER_ADDR", "127.0.0.1")
+            td.init_process_group("gloo")
+            self.td = td
+
+    def barrier(self):
+        if self.world > 1:
+            self.td.barrier()
+
+    def max(self, x):
+        if self.world == 1:
+            return x
+        import torch
+        t = torch.tensor([float(x)], dtype=torch.float64)
+        self.td.all_reduce(t, op=self.td.ReduceOp.MAX)
+        return float(t.item())
+
+
+def workload(L, nlayers, nsteps, seed=3):
+    import targets as T
+    import numpy as np
+    g, w, _ = T.hubbard_trotter_circuit(L // 2, 1.0, 4.0, 0.25, nsteps)
+    rng = np.random.default_rng(seed)
+    v = T.near_identity_brickwall(nlayers, rng)
+    perms = T.brickwall_perms(L, nlayers)
+    return g, w, v, perms
+
+
+def alg_flops(L, gu, gw, ncols):
+    """algorithmic real flops of target+gradient over ncols columns, counted on the parity
+    sector S = 2^(L-1): 14 per amplitude and forward gate, 44 per amplitude and fitted gate
+    (forward 14 + backward 30), 8 per amplitude for the overlap"""
+    return float(ncols) * (1 << (L - 1)) * (14 * gu + 44 * gw + 8)
+
+
+class Clocks:
+    """nvidia-smi samples during the timed region"""
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+         "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device):
+        self.device = device
+        self.f = tempfile.NamedTemporaryFile("w+", suffix=".csv", delete=False)
+        self.p = None
+
+    def start(self):
+        try:
+            self.p = subprocess.Popen(["nvidia-smi", "-i", str(self.device), f"--query-gpu={self.Q}", "--format=csv,noheader,nounits",
+                                       "-lms", "200"], stdout=self.f, stderr=subprocess.DEVNULL)
+        except OSError:
+            self.p = None
+
+    def stop(self):
+        if not self.p:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.p.terminate()
+        self.p.wait()
+        self.f.seek(0)
+        rows = [r.split(",") for r in self.f.read().strip().splitlines() if r.strip()]
+        os.unlink(self.f.name)
+        sm, smax, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for r in rows:
+            try:
+                sm.append(float(r[1])); smax = float(r[2])
+                for n, v in zip(names, r[5:9]):
+                    if v.strip().lower() in ("active", "1"):
+                        reasons.add(n)
+            except (ValueError, IndexError):
+                pass
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": smax, "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def cpu_baseline(g, w, v, perms, L, budget_s, nthreads=0):
+    """the oracle port (reference algorithm, full vectors, OpenMP over basis columns) on a
+    bounded column sample; returns (evals/s, threads, columns, seconds)"""
+    import oracle
+    nthreads = nthreads or os.cpu_count()
+    t = oracle.Target("circuit", L, gates=g, wires=w)
+    ncols = nthreads
+    t0 = time.perf_counter()
+    oracle.brickwall_projected_gradient(t, v, perms, L, nthreads=nthreads, col_range=(0, ncols))
+    dt = time.perf_counter() - t0
+    reps = max(1, min(64, int(budget_s / max(dt, 1e-3))))
+    if reps > 1:
+        ncols = nthreads * reps
+        t0 = time.perf_counter()
+        oracle.brickwall_projected_gradient(t, v, perms, L, nthreads=nthreads, col_range=(0, ncols))
+        dt = time.perf_counter() - t0
+    return (ncols / float(1 << L)) / dt, nthreads, ncols, dt
+
+
+def run_reference(a):
+    rank, world, _ = dist_env()
+    if rank != 0:
+        return
+    g, w, v, perms = workload(a.L, a.layers, a.trotter_steps)
+    import oracle
+    nthreads = os.cpu_count()
+    t = oracle.Target("circuit", a.L, gates=g, wires=w)
+    # size the per-step column sample to a few seconds of host work
+    t0 = time.perf_counter()
+    oracle.brickwall_projected_gradient(t, v, perms, a.L, nthreads=nthreads, col_range=(0, nthreads))
+    d1 = time.perf_counter() - t0
+    ncols = nthreads * max(1, min(64, int(5.0 / max(d1, 1e-3))))
+    for _ in range(max(0, a.warmup - 1)):
+        oracle.brickwall_projected_gradient(t, v, perms, a.L, nthreads=nthreads, col_range=(0, nthreads))
+    times = []
+    for _ in range(a.steps):
+        t0 = time.perf_counter()
+        oracle.brickwall_projected_gradient(t, v, perms, a.L, nthreads=nthreads, col_range=(0, ncols))
+        times.append(time.perf_counter() - t0)
+    sec_per_eval = statistics.mean(times) * (1 << a.L) / ncols
+    value = 1.0 / sec_per_eval
+    sample = f"{ncols} of {1 << a.L} basis columns per step, scaled to one full gradient evaluation"
+    print(json.dumps({
+        "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": a.gpus, "steps": a.steps, "warmup": a.warmup,
+        "ms_per_step": sec_per_eval * 1e3, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f64", "data": "synthetic (seeded Hubbard Trotter target)",
+        "config": {"workload": f"L={a.L} spinful Hubbard Trotter target ({len(g)} gates), {a.layers}-layer brickwall fit, target+gradient",
+                   "L": a.L, "nlayers": a.layers, "target_gates": len(g)},
+        "cpu_baseline": {"value": value, "unit": UNIT, "cores": nthreads, "kind": "port", "sample": sample},
+        "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }))
+
+
+def run_gb300(a):
+    import numpy as np
+    rank, world, local = dist_env()
+    os.environ["MG_DEVICE"] = str(local)
+    dist = Dist(world)
+    import mgcu
+    lib = mgcu.default_lib()
+    prec = {"mixed": mgcu.PREC_MIXED, "fp64": mgcu.PREC_FP64, "fp32": mgcu.PREC_FP32}[a.precision]
+    L, nl = a.L, a.layers
+    g, w, v, perms = workload(L, nl, a.trotter_steps)
+    gu, gw = len(g), nl * (L // 2)
+    ncols = 1 << L
+    fp32_peak = lib.lib.mg_measure_fp32_peak_gflops()
+    fp64_peak = lib.lib.mg_measure_fp64_peak_gflops()
+
+    target = lib.target_circuit(g, w, L)
+    lib.set_precision(prec)
+    plan = lib.plan_brickwall(lib.mg_target_apply, target, v, perms, L, mgcu.EVAL_GRADIENT)
+    for _ in range(a.warmup):
+        assert lib.lib.mg_plan_run(mgcu.P(plan)) == 0, lib.last_error()
+    dist.barrier()
+    clocks = Clocks(local)
+    clocks.start()
+    n0 = lib.launch_count()
+    total_ms = lib.lib.mg_plan_time_ms(mgcu.P(plan), a.steps, 1)
+    launches = lib.launch_count() - n0
+    clk = clocks.stop()
+    dist.barrier()
+    assert total_ms > 0, lib.last_error()
+    f_dev, dv_dev, _, gvec_dev, _ = lib.plan_results(plan, nl, grad=True, proj=True)
+    total_s = dist.max(total_ms / 1e3)
+    value = world * a.steps / total_s
+    ms_per_step = total_s * 1e3 / a.steps
+
+    # end to end through the reference-facing C call, host buffers in and out
+    for _ in range(1):
+        lib.brickwall_projected_gradient(lib.mg_target_apply, target, v, perms, L)
+    dist.barrier()
+    e2e_t = []
+    for _ in range(a.steps):
+        t0 = time.perf_counter()
+        rc, f_e2e, g_e2e = lib.brickwall_projected_gradient(lib.mg_target_apply, target, v, perms, L)
+        e2e_t.append(time.perf_counter() - t0)
+        assert rc == 0, lib.last_error()
+    e2e_s = dist.max(sum(e2e_t))
+    tsize = 16 if prec != mgcu.PREC_FP32 else 8
+    h2d = gu * 0 + (nl * (L // 2)) * 8 * tsize + nl * 128      # gate matrices + gates for the projection
+    d2h = 16 + nl * 8 * 8                                      # f + projected gradient
+
+    # FP64 on a column sample: time and accuracy of the timed precision against it
+    c = min(a.fp64_columns, ncols)
+    lib.set_precision(mgcu.PREC_FP64)
+    lib.brickwall_columns(lib.mg_target_apply, target, v, perms, L, 0, min(64, c))
+    t0 = time.perf_counter()
+    rc, f64, dv64 = lib.brickwall_columns(lib.mg_target_apply, target, v, perms, L, 0, c)
+    t64 = time.perf_counter() - t0
+    lib.set_precision(prec)
+    rc2, fx, dvx = lib.brickwall_columns(lib.mg_target_apply, target, v, perms, L, 0, c)
+    fp64_value = (c / ncols) / t64
+    rel_f = abs(fx - f64) / abs(f64)
+    rel_g = float(np.linalg.norm(dvx - dv64) / np.linalg.norm(dv64))
+
+    flops = alg_flops(L, gu, gw, ncols)
+    achieved = flops / (ms_per_step / 1e3) / 1e12
+    out = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": a.steps, "warmup": a.warmup,
+        "ms_per_step": ms_per_step, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": {"mixed": "f32 float-float pairs (about 48-bit significands), f64 final sums",
+                  "fp64": "f64", "fp32": "f32, compensated f32 sums"}[a.precision],
+        "data": "synthetic (seeded Hubbard Trotter target, seeded near-identity fit)",
+        "config": {"workload": f"L={L} spinful Hubbard Trotter target ({gu} gates, 64 second-order steps), "
+                               f"{nl}-layer brickwall fit ({gw} gates), f + gate gradients over all 2^{L} columns",
+                   "L": L, "nlayers": nl, "target_gates": gu, "precision": a.precision,
+                   "l2": "a 512 MiB buffer is written between timed steps; per-step working set also exceeds L2",
+                   "parallelism": f"replicas x{world}"},
+        "gpu_launches": launches,
+        "clocks": clk,
+        "e2e": {"value": world * a.steps / e2e_s, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
+                "timer": "host clock around matchgate_brickwall_unitary_target_and_projected_gradient (synchronous C call)"},
+        "roofline": {"bound": "fp32", "achieved": achieved, "peak": fp32_peak / 1e3, "unit": "TFLOP/s",
+                     "frac": achieved / (fp32_peak / 1e3), "traffic": None,
+                     "achieved_is": "algorithmic complex-arithmetic flops (parity sector) per second",
+                     "peak_source": "FP32 FMA microkernel of this library, measured in this run",
+                     "fp64_peak_tflops": fp64_peak / 1e3},
+        "fp64_gpu": {"value": fp64_value, "unit": UNIT, "sample_columns": c, "extrapolated_from_sample": True,
+                     "speedup_of_timed_precision": value / world / fp64_value},
+        "accuracy": {"rel_err_f_vs_fp64": rel_f, "rel_err_grad_vs_fp64": rel_g, "columns": c,
+                     "f": [float(np.real(f_dev)), float(np.imag(f_dev))]},
+        "serving": None,
+    }
+    if rank == 0 and world == 1 and not a.no_cpu:
+        cv, cores, cc, cs = cpu_baseline(g, w, v, perms, L, a.cpu_seconds)
+        out["cpu_baseline"] = {"value": cv, "unit": UNIT, "cores": cores, "kind": "port",
+                               "sample": f"{cc} of {ncols} basis columns in {cs:.1f} s, scaled to one full evaluation"}
+    lib.lib.mg_plan_free(mgcu.P(plan))
+    lib.target_free(target)
+    if rank == 0:
+        print(json.dumps(out))
+
+
+def main():
+    a = parse()
+    if a.impl == "reference":
+        run_reference(a)
+    else:
+        run_gb300(a)
+
+
+if __name__ == "__main__":
+    main()

@@ -67,7 +67,7 @@ def build(force=False, verbose=False):
         raise RuntimeError("building libmgcu.so failed")
     objs = [_obj(s) for s in cu + c]
     if force or jobs or _stale(LIB, objs):
-        cmd = [NVCC] + ARCH + ["-shared", "-o", LIB] + objs + ["-lcudart", "-lpthread", "-lm"]
+        cmd = [NVCC] + ARCH + ["-shared", "-o", LIB] + objs + ["-lpthread", "-lm"]
         r = subprocess.run(cmd, capture_output=True, text=True)
         if r.returncode != 0:
             sys.stderr.write(" ".join(cmd) + "\n" + r.stdout + r.stderr)

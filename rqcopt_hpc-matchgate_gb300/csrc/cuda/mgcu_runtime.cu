@@ -3,6 +3,7 @@
 #include "mgcu_common.cuh"
 
 #include <atomic>
+#include <stdlib.h>
 
 static MgcuContext g_ctx;
 static int g_ctx_state = 0;   // 0 uninitialised, 1 ready, -1 failed
@@ -26,11 +27,14 @@ MgcuContext* mgcu_ctx()
 		g_ctx_state = -1;
 		return nullptr;
 	}
-	g_ctx.device = 0;
+	// MG_DEVICE selects the GPU (one process per GPU; default 0)
+	const char* env = getenv("MG_DEVICE");
+	g_ctx.device = env ? atoi(env) : 0;
 	cudaDeviceProp prop;
-	if (cudaSetDevice(0) != cudaSuccess || cudaGetDeviceProperties(&prop, 0) != cudaSuccess)
+	if (g_ctx.device < 0 || g_ctx.device >= ndev || cudaSetDevice(g_ctx.device) != cudaSuccess ||
+		cudaGetDeviceProperties(&prop, g_ctx.device) != cudaSuccess)
 	{
-		mg_set_error("cannot open CUDA device 0");
+		mg_set_error("cannot open CUDA device %d (of %d)", g_ctx.device, ndev);
 		g_ctx_state = -1;
 		return nullptr;
 	}

@@ -1,0 +1,98 @@
+"""Mixed and FP32 precision against the FP64 path, and the trust-region optimiser
+against the oracle's restatement of the reference's (src/trust_region.c:235-306 driven
+as in src/mg_brickwall_opt.c:99-122)."""
+import numpy as np
+import pytest
+
+import mgcu
+import targets as T
+from conftest import brickwall_perms, random_gates, rel, udist
+
+pytestmark = pytest.mark.gpu
+
+# stated tolerances: relative 2-norm error against the FP64 result
+TOL_MIXED = 1e-9
+TOL_FP32 = 1e-4
+
+
+@pytest.fixture(scope="module")
+def lib(mglib):
+    for o in (1, 2, 3, 4):
+        mglib.set_option(o, 0)
+    yield mglib
+    mglib.set_precision(mgcu.PREC_FP64)
+
+
+def _hubbard(lib, L):
+    g, w, _ = T.hubbard_trotter_circuit(L // 2, 1.0, 4.0, 0.25, 16)
+    return lib.target_circuit(g, w, L)
+
+
+@pytest.mark.parametrize("L,tile_bits", [(8, 0), (10, 0), (12, 0), (12, 7)])
+def test_mixed_and_fp32_gradient(lib, L, tile_bits):
+    rng = np.random.default_rng(L)
+    nl = 5
+    v = T.near_identity_brickwall(nl, rng)
+    perms = T.brickwall_perms(L, nl)
+    t = _hubbard(lib, L)
+    lib.set_option(mgcu.OPT_TILE_BITS, tile_bits)
+    try:
+        out = {}
+        for p in (mgcu.PREC_FP64, mgcu.PREC_MIXED, mgcu.PREC_FP32):
+            lib.set_precision(p)
+            rc, f, g = lib.brickwall_projected_gradient(lib.mg_target_apply, t, v, perms, L)
+            rc2, f2, dv = lib.brickwall_target_and_gradient(lib.mg_target_apply, t, v, perms, L)
+            assert rc == 0 and rc2 == 0
+            out[p] = (f, g, dv)
+    finally:
+        lib.set_option(mgcu.OPT_TILE_BITS, 0)
+        lib.set_precision(mgcu.PREC_FP64)
+        lib.target_free(t)
+    f64, g64, dv64 = out[mgcu.PREC_FP64]
+    fm, gm, dvm = out[mgcu.PREC_MIXED]
+    assert abs(fm - f64) / abs(f64) < TOL_MIXED
+    assert rel(dvm, dv64) < TOL_MIXED
+    assert rel(gm, g64) < 1e-6   # the projected gradient is small near identity: absolute 1e-9 scale
+    assert np.max(np.abs(gm - g64)) < 1e-9 * np.max(np.abs(dv64))
+    ff, gf, dvf = out[mgcu.PREC_FP32]
+    assert abs(ff - f64) / abs(f64) < TOL_FP32 and rel(dvf, dv64) < TOL_FP32
+
+
+def test_mixed_hessian(lib):
+    rng = np.random.default_rng(5)
+    L, nl = 8, 4
+    v = random_gates(nl, rng, unitary=True)
+    perms = brickwall_perms(L, nl)
+    t = lib.target_brickwall(random_gates(8, rng, unitary=True), brickwall_perms(L, 8, rng), L)
+    try:
+        lib.set_precision(mgcu.PREC_FP64)
+        rc, f, g, H = lib.brickwall_gradvec_hessmat(lib.mg_target_apply, t, v, perms, L)
+        lib.set_precision(mgcu.PREC_MIXED)
+        rc2, fm, gm, Hm = lib.brickwall_gradvec_hessmat(lib.mg_target_apply, t, v, perms, L)
+    finally:
+        lib.set_precision(mgcu.PREC_FP64)
+        lib.target_free(t)
+    assert rc == 0 and rc2 == 0
+    assert abs(fm - f) / abs(f) < TOL_MIXED and rel(gm, g) < TOL_MIXED and rel(Hm, H) < TOL_MIXED
+
+
+def test_trust_region_matches_oracle(lib, oracle):
+    """10 trust-region iterations at L=8 (4 layers) against a depth-8 random matchgate
+    brickwall target: every iterate's f equals the oracle's"""
+    rng = np.random.default_rng(1)
+    L, nl, ul = 8, 4, 8
+    perms = brickwall_perms(L, nl)
+    uperms = brickwall_perms(L, ul)
+    ulist = random_gates(ul, rng, unitary=True)
+    v0 = random_gates(nl, rng, unitary=True)
+    niter = 10
+    lib.set_precision(mgcu.PREC_FP64)
+    t = lib.target_brickwall(ulist, uperms, L)
+    try:
+        f_g, fc_g, v_g = lib.optimize_brickwall(lib.mg_target_apply, t, v0, perms, L, niter)
+    finally:
+        lib.target_free(t)
+    f_o, fc_o, v_o = oracle.rtr_brickwall(oracle.Target("brickwall", L, ulist=ulist, uperms=uperms), v0, perms, L, niter)
+    assert np.max(np.abs(f_g - f_o)) < 1e-8
+    assert udist(v_g, v_o) < 1e-8
+    assert f_g[-1] < f_g[0]
