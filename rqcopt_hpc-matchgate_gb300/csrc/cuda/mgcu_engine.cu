@@ -1248,3 +1248,191 @@ extern "C" double mgcu_plan_time_ms(mgcu_plan* p, long b0, long b1, int steps, i
 	}
 	return total;
 }
+
+// ======================================================================================
+// Allocation-free evaluation: f and layer gradients of a brickwall against a target
+// circuit, with every workspace in one fixed device array instead of cudaMalloc'd
+// buffers.  For callers that must not allocate GPU memory mid-run (see mg_gb300.h).
+// ======================================================================================
+namespace {
+
+constexpr int NA_MAX_QUBITS = 10;          // one shared-memory tile holds a whole sector
+constexpr int NA_MAX_FIT_GATES = 64;       // nlayers * nqubits / 2
+constexpr int NA_MAX_TARGET_GATES = 4096;
+constexpr int NA_BLOCKS = 64;              // resident columns at a time
+constexpr size_t NA_S = (size_t)1 << (NA_MAX_QUBITS - 1);
+
+// byte offsets inside the scratch array (every region 256-byte aligned)
+constexpr size_t na_al(size_t x) { return (x + 255) / 256 * 256; }
+constexpr size_t NA_SU = 0;
+constexpr size_t NA_SW = NA_SU + na_al(sizeof(double2) * NA_BLOCKS * NA_S);
+constexpr size_t NA_CACHE = NA_SW + na_al(sizeof(double2) * NA_BLOCKS * NA_S);
+constexpr size_t NA_PART_F = NA_CACHE + na_al(sizeof(double2) * NA_BLOCKS * NA_MAX_FIT_GATES * NA_S);
+constexpr size_t NA_PART_G = NA_PART_F + na_al(sizeof(double) * 2 * NA_BLOCKS);
+constexpr size_t NA_OUT_F = NA_PART_G + na_al(sizeof(double) * 16 * NA_MAX_FIT_GATES * NA_BLOCKS);
+constexpr size_t NA_OUT_G = NA_OUT_F + na_al(sizeof(double) * 2);
+constexpr size_t NA_OUT_BLK = NA_OUT_G + na_al(sizeof(double) * 16 * NA_MAX_FIT_GATES);
+constexpr size_t NA_WMAT = NA_OUT_BLK + na_al(sizeof(double) * 16 * NA_MAX_FIT_GATES);
+constexpr size_t NA_UMAT = NA_WMAT + na_al(sizeof(double2) * 8 * NA_MAX_FIT_GATES);
+constexpr size_t NA_PASS = NA_UMAT + na_al(sizeof(double2) * 8 * NA_MAX_TARGET_GATES);
+constexpr size_t NA_GATE = NA_PASS + na_al(sizeof(PassRec) * 2);
+constexpr size_t NA_BLOCK = NA_GATE + na_al(sizeof(GateRec) * (NA_MAX_FIT_GATES + NA_MAX_TARGET_GATES));
+constexpr size_t NA_BYTES = NA_BLOCK + na_al(sizeof(int) * NA_MAX_FIT_GATES);
+
+// host staging for the small inputs: static storage, no heap
+PassRec na_pass_h[2];
+GateRec na_gate_h[NA_MAX_FIT_GATES + NA_MAX_TARGET_GATES];
+double2 na_wmat_h[8 * NA_MAX_FIT_GATES];
+double2 na_umat_h[8 * NA_MAX_TARGET_GATES];
+int na_block_h[NA_MAX_FIT_GATES];
+int na_wires_h[2 * NA_MAX_FIT_GATES];
+double na_out_h[2 + 16 * NA_MAX_FIT_GATES];
+unsigned char* na_base[64];                // scratch address per device, set at first use
+
+// one pass with every compact bit local (the sector fits one tile)
+void na_single_pass(int L, const int* wires, int ng, int gofs, PassRec& pr, GateRec* recs)
+{
+	const int nb = L - 1;
+	memset(&pr, 0, sizeof(pr));
+	for (int b = 0; b < nb; b++) pr.lbits[b] = b;
+	pr.nnl = 0;
+	pr.gbeg = gofs;
+	pr.gend = gofs + ng;
+	for (int g = 0; g < ng; g++)
+	{
+		GateRec r;
+		const int a = compact_bit(L, wires[2 * g]), b = compact_bit(L, wires[2 * g + 1]);
+		r.g = g;
+		r.type = (a >= 0 && b >= 0) ? 0 : (b < 0 ? 1 : 2);
+		r.la = a;
+		r.lb = b;
+		const int used = r.type == 1 ? r.la : r.lb;
+		r.lc = (used == 0) ? 1 : 0;
+		recs[gofs + g] = r;
+	}
+}
+
+}  // namespace
+
+// Every GPU that loads this library reserves this array until the process exits.
+static __device__ __align__(256) unsigned char g_noalloc_scratch[NA_BYTES];
+
+// C linkage: the types of mg_gb300.h's declaration (struct matchgate, numeric) share these layouts
+extern "C" int mg_noalloc_brickwall_target_and_gradient(const void* ugates, int ungates, const int uwires[],
+	const void* vlist, int nlayers, int nqubits, const int* perms[], double* fval, void* dvlist)
+{
+	const int L = nqubits, half = L / 2, ng = nlayers * half;
+	if (L < 4 || L > NA_MAX_QUBITS || L % 2 || nlayers < 1 || ng > NA_MAX_FIT_GATES || ungates < 0 || ungates > NA_MAX_TARGET_GATES)
+	{
+		mg_set_error("mg_noalloc_brickwall_target_and_gradient: sizes outside its fixed workspace (need even 4 <= nqubits <= %d, "
+			"nlayers*nqubits/2 <= %d, target gates <= %d; got nqubits=%d nlayers=%d target gates=%d)",
+			NA_MAX_QUBITS, NA_MAX_FIT_GATES, NA_MAX_TARGET_GATES, L, nlayers, ungates);
+		return MG_ERR_ARG;
+	}
+	for (int g = 0; g < 2 * ungates; g++)
+		if (uwires[g] < 0 || uwires[g] >= L || (g % 2 && uwires[g] == uwires[g - 1]))
+		{
+			mg_set_error("mg_noalloc_brickwall_target_and_gradient: invalid wires of target gate %d", g / 2);
+			return MG_ERR_ARG;
+		}
+	for (int i = 0; i < nlayers; i++)
+		for (int p = 0; p < L; p++)
+			if (perms[i][p] < 0 || perms[i][p] >= L)
+			{
+				mg_set_error("mg_noalloc_brickwall_target_and_gradient: invalid permutation of layer %d", i);
+				return MG_ERR_ARG;
+			}
+	mgcu_lock();
+	MgcuContext* c = mgcu_ctx();
+	if (!c) { mgcu_unlock(); return MG_ERR_DEVICE; }
+	int rc = 0;
+	// set-up once per device, with that device current: the device address of the array
+	if (!na_base[c->device])
+	{
+		void* p = nullptr;
+		cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+		if (e != cudaSuccess) { rc = mgcu_check(e, "cudaGetSymbolAddress", __FILE__, __LINE__); mgcu_unlock(); return rc; }
+		na_base[c->device] = (unsigned char*)p;
+	}
+	unsigned char* base = na_base[c->device];
+	const mgg* W = reinterpret_cast<const mgg*>(vlist);
+	const mgg* U = reinterpret_cast<const mgg*>(ugates);
+	for (int i = 0; i < nlayers; i++)
+		for (int p = 0; p < half; p++)
+		{
+			const int g = i * half + p;
+			na_wires_h[2 * g] = perms[i][2 * p];
+			na_wires_h[2 * g + 1] = perms[i][2 * p + 1];
+			na_block_h[g] = i;
+			for (int q = 0; q < 4; q++)
+			{
+				na_wmat_h[8 * g + q] = make_double2(W[i].c[q].re, W[i].c[q].im);
+				na_wmat_h[8 * g + 4 + q] = make_double2(W[i].k[q].re, W[i].k[q].im);
+			}
+		}
+	for (int g = 0; g < ungates; g++)
+		for (int q = 0; q < 4; q++)
+		{
+			na_umat_h[8 * g + q] = make_double2(U[g].c[q].re, U[g].c[q].im);
+			na_umat_h[8 * g + 4 + q] = make_double2(U[g].k[q].re, U[g].k[q].im);
+		}
+	na_single_pass(L, na_wires_h, ng, 0, na_pass_h[0], na_gate_h);
+	na_single_pass(L, uwires, ungates, ng, na_pass_h[1], na_gate_h);
+	cudaStream_t st = c->stream;
+	const long ncols = 1L << L;
+	const int grid = (int)std::min<long>(NA_BLOCKS, ncols);
+	const int kt = L - 1;
+	const int threads = std::max(32, std::min(256, 1 << (kt - 2)));
+	const size_t smem = ((size_t)1 << kt) * sizeof(double2) + 2 * 128 * sizeof(unsigned) + (size_t)(threads / 32) * 16 * sizeof(double);
+#define NA_TRY(x) do { cudaError_t _e = (x); if (_e != cudaSuccess) { rc = mgcu_check(_e, #x, __FILE__, __LINE__); goto done; } } while (0)
+	NA_TRY(cudaMemcpyAsync(base + NA_WMAT, na_wmat_h, sizeof(double2) * 8 * ng, cudaMemcpyHostToDevice, st));
+	if (ungates) NA_TRY(cudaMemcpyAsync(base + NA_UMAT, na_umat_h, sizeof(double2) * 8 * ungates, cudaMemcpyHostToDevice, st));
+	NA_TRY(cudaMemcpyAsync(base + NA_PASS, na_pass_h, sizeof(PassRec) * 2, cudaMemcpyHostToDevice, st));
+	NA_TRY(cudaMemcpyAsync(base + NA_GATE, na_gate_h, sizeof(GateRec) * (ng + ungates), cudaMemcpyHostToDevice, st));
+	NA_TRY(cudaMemcpyAsync(base + NA_BLOCK, na_block_h, sizeof(int) * ng, cudaMemcpyHostToDevice, st));
+	// the partial sums accumulate: clear them (the array keeps the previous call's contents)
+	NA_TRY(cudaMemsetAsync(base + NA_PART_F, 0, sizeof(double) * 2 * NA_BLOCKS, st));
+	NA_TRY(cudaMemsetAsync(base + NA_PART_G, 0, sizeof(double) * 16 * ng * NA_BLOCKS, st));
+	{
+		Args<PrecD> a;
+		memset(&a, 0, sizeof(a));
+		a.L = L; a.nb = L - 1; a.kt = kt; a.S = ncols >> 1;
+		a.W.pass = reinterpret_cast<const PassRec*>(base + NA_PASS);
+		a.W.gate = reinterpret_cast<const GateRec*>(base + NA_GATE);
+		a.W.npass = 1;
+		a.U.pass = reinterpret_cast<const PassRec*>(base + NA_PASS) + 1;
+		a.U.gate = reinterpret_cast<const GateRec*>(base + NA_GATE);
+		a.U.npass = 1;
+		a.wm = reinterpret_cast<const double2*>(base + NA_WMAT);
+		a.um = reinterpret_cast<const double2*>(base + NA_UMAT);
+		a.ngates = ng;
+		a.b0 = 0; a.b1 = ncols;
+		a.su = reinterpret_cast<double2*>(base + NA_SU);
+		a.sw = reinterpret_cast<double2*>(base + NA_SW);
+		a.cache = reinterpret_cast<double2*>(base + NA_CACHE);
+		a.want_grad = 1;
+		a.part_f = reinterpret_cast<double*>(base + NA_PART_F);
+		a.part_g = reinterpret_cast<double*>(base + NA_PART_G);
+		k_columns<PrecD><<<grid, threads, smem, st>>>(a);
+		mgcu_count_launch();
+		NA_TRY(cudaGetLastError());
+		k_sum_parts<<<1, 32, 0, st>>>(a.part_f, grid, 2, reinterpret_cast<double*>(base + NA_OUT_F));
+		mgcu_count_launch();
+		k_sum_parts<<<grid_cap(16L * ng, 128), 128, 0, st>>>(a.part_g, grid, 16L * ng, reinterpret_cast<double*>(base + NA_OUT_G));
+		mgcu_count_launch();
+		k_block_sum<<<(16 * nlayers + 127) / 128, 128, 0, st>>>(reinterpret_cast<double*>(base + NA_OUT_G), reinterpret_cast<const int*>(base + NA_BLOCK),
+			ng, nlayers, reinterpret_cast<double*>(base + NA_OUT_BLK));
+		mgcu_count_launch();
+		NA_TRY(cudaGetLastError());
+	}
+	NA_TRY(cudaMemcpyAsync(na_out_h, base + NA_OUT_F, sizeof(double) * 2, cudaMemcpyDeviceToHost, st));
+	NA_TRY(cudaMemcpyAsync(na_out_h + 2, base + NA_OUT_BLK, sizeof(double) * 16 * nlayers, cudaMemcpyDeviceToHost, st));
+	NA_TRY(cudaStreamSynchronize(st));
+	fval[0] = na_out_h[0];
+	fval[1] = na_out_h[1];
+	memcpy(dvlist, na_out_h + 2, sizeof(double) * 16 * nlayers);
+done:
+#undef NA_TRY
+	mgcu_unlock();
+	return rc;
+}
