@@ -121,6 +121,15 @@ struct PrecD
 		return r;
 	}
 	__device__ static T negconj(T a) { return make_double2(-a.x, a.y); }
+	__device__ static T neg(T a) { return make_double2(-a.x, -a.y); }
+	__device__ static T mul(T a, T x) { return make_double2(fma(a.x, x.x, -a.y * x.y), fma(a.x, x.y, a.y * x.x)); }
+	// a x + b y for entries that are real or imaginary: a = (c_re, c_im) with c_re, c_im the
+	// coefficients of the (possibly swapped) components of x; swap when the entry is imaginary
+	__device__ static T madd2_ri(T a, bool ra, T x, T b, bool rb, T y)
+	{
+		const double xr = ra ? x.y : x.x, xi = ra ? x.x : x.y, yr = rb ? y.y : y.x, yi = rb ? y.x : y.y;
+		return make_double2(fma(a.x, xr, b.x * yr), fma(a.y, xi, b.y * yi));
+	}
 	__device__ static Acc acc_zero() { Acc a; a.re = 0; a.im = 0; return a; }
 	__device__ static void acc_mul_add(Acc& s, T d, T x)
 	{
@@ -154,6 +163,13 @@ struct PrecF
 		return r;
 	}
 	__device__ static T negconj(T a) { return make_float2(-a.x, a.y); }
+	__device__ static T neg(T a) { return make_float2(-a.x, -a.y); }
+	__device__ static T mul(T a, T x) { return make_float2(fmaf(a.x, x.x, -a.y * x.y), fmaf(a.x, x.y, a.y * x.x)); }
+	__device__ static T madd2_ri(T a, bool ra, T x, T b, bool rb, T y)
+	{
+		const float xr = ra ? x.y : x.x, xi = ra ? x.x : x.y, yr = rb ? y.y : y.x, yi = rb ? y.x : y.y;
+		return make_float2(fmaf(a.x, xr, b.x * yr), fmaf(a.y, xi, b.y * yi));
+	}
 	__device__ static Acc acc_zero() { Acc a; a.rh = a.rl = a.ih = a.il = 0.f; return a; }
 	__device__ static void acc_mul_add(Acc& s, T d, T x)
 	{
@@ -207,6 +223,35 @@ struct PrecX
 		return r;
 	}
 	__device__ static T negconj(T a) { return make_float4(-a.x, a.y, -a.z, a.w); }
+	__device__ static T neg(T a) { return make_float4(-a.x, -a.y, -a.z, -a.w); }
+	// a x as two 2-term compensated dot products
+	__device__ static T mul(T a, T x)
+	{
+		float rh, rl, ih, il, s, t;
+		ff_prod(a.x, a.z, x.x, x.z, rh, rl);
+		ff_acc_prod(rh, rl, -a.y, -a.w, x.y, x.w);
+		ff_prod(a.x, a.z, x.y, x.w, ih, il);
+		ff_acc_prod(ih, il, a.y, a.w, x.x, x.z);
+		T r;
+		fast_two_sum(rh, rl, s, t); r.x = s; r.z = t;
+		fast_two_sum(ih, il, s, t); r.y = s; r.w = t;
+		return r;
+	}
+	// a x + b y for real-or-imaginary entries (see PrecD::madd2_ri): 2-term dots per part
+	__device__ static T madd2_ri(T a, bool ra, T x, T b, bool rb, T y)
+	{
+		const float xrh = ra ? x.y : x.x, xrl = ra ? x.w : x.z, xih = ra ? x.x : x.y, xil = ra ? x.z : x.w;
+		const float yrh = rb ? y.y : y.x, yrl = rb ? y.w : y.z, yih = rb ? y.x : y.y, yil = rb ? y.z : y.w;
+		float rh, rl, ih, il, s, t;
+		ff_prod(a.x, a.z, xrh, xrl, rh, rl);
+		ff_acc_prod(rh, rl, b.x, b.z, yrh, yrl);
+		ff_prod(a.y, a.w, xih, xil, ih, il);
+		ff_acc_prod(ih, il, b.y, b.w, yih, yil);
+		T r;
+		fast_two_sum(rh, rl, s, t); r.x = s; r.z = t;
+		fast_two_sum(ih, il, s, t); r.y = s; r.w = t;
+		return r;
+	}
 	__device__ static Acc acc_zero() { return PrecF::acc_zero(); }
 	__device__ static void acc_mul_add(Acc& s, T d, T x)
 	{

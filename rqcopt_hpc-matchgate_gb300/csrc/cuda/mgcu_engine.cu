@@ -179,6 +179,7 @@ struct Args
 	ProgDev W, U;
 	const T* wm;               // W gate matrices [ngates][8]: c0..c3, k0..k3
 	const T* um;               // target gate matrices
+	const int* ukind;          // target block kinds (null: every block general)
 	int ngates;
 	const T* dense;            // -conj(U e_b) columns, or null (then U is run)
 	long dense_b0;
@@ -410,6 +411,56 @@ __device__ __forceinline__ void gate_forward(typename P::T* tile, const GateRec&
 	}
 }
 
+// Structured blocks of target gates, classified exactly on the host (see classify_block):
+// identity blocks are skipped, swaps move data, diagonal blocks multiply once, and blocks
+// whose entries are each real or imaginary take 2-term instead of 4-term dot products.
+enum { BK_ID = 0, BK_SWAP = 1, BK_D1 = 2, BK_NEG1 = 3, BK_DIAG = 4, BK_ANTI = 5, BK_RI = 6, BK_GEN = 7 };
+
+template <class P>
+__device__ __forceinline__ void pair_kind(typename P::T* tile, unsigned p0, unsigned p1, int kind, unsigned rot,
+	const typename P::T& m0, const typename P::T& m1, const typename P::T& m2, const typename P::T& m3)
+{
+	typedef typename P::T T;
+	switch (kind)
+	{
+	case BK_ID: return;
+	case BK_SWAP: { const T a = tile[p0], b = tile[p1]; tile[p0] = b; tile[p1] = a; return; }
+	case BK_D1: tile[p1] = P::mul(m3, tile[p1]); return;
+	case BK_NEG1: tile[p1] = P::neg(tile[p1]); return;
+	case BK_DIAG: tile[p0] = P::mul(m0, tile[p0]); tile[p1] = P::mul(m3, tile[p1]); return;
+	case BK_ANTI: { const T a = tile[p0], b = tile[p1]; tile[p0] = P::mul(m1, b); tile[p1] = P::mul(m2, a); return; }
+	case BK_RI:
+	{
+		const T a = tile[p0], b = tile[p1];
+		tile[p0] = P::madd2_ri(m0, rot & 1, a, m1, rot & 2, b);
+		tile[p1] = P::madd2_ri(m2, rot & 4, a, m3, rot & 8, b);
+		return;
+	}
+	default:
+	{
+		const T a = tile[p0], b = tile[p1];
+		tile[p0] = P::madd2(m0, a, m1, b);
+		tile[p1] = P::madd2(m2, a, m3, b);
+	}
+	}
+}
+
+// forward application of a target gate with classified blocks; kw = kind word
+// (center kind | corner kind << 3 | center rot bits << 6 | corner rot bits << 10)
+template <class P>
+__device__ __forceinline__ void gate_forward_kinds(typename P::T* tile, const GateRec& r, const Gate8<typename P::T>& G, int kw, int Q, int tpar)
+{
+	const int kc = kw & 7, kk = (kw >> 3) & 7;
+	const unsigned rc = (kw >> 6) & 15, rk = (kw >> 10) & 15;
+	for (unsigned q = threadIdx.x; q < (unsigned)Q; q += blockDim.x)
+	{
+		unsigned ex, ew, ey, ez;
+		quartet(r, q, tpar, ex, ew, ey, ez);
+		pair_kind<P>(tile, ex, ew, kk, rk, G.k0, G.k1, G.k2, G.k3);
+		pair_kind<P>(tile, ey, ez, kc, rc, G.c0, G.c1, G.c2, G.c3);
+	}
+}
+
 // contraction of the derivative d (state after the gate, read from dsrc) with the
 // state before the gate x: acc[e] += d_r x_s for the 8 block entries
 template <class P>
@@ -450,7 +501,7 @@ __device__ __forceinline__ void tile_store(const typename P::T* tile, int kt, co
 // ends in slot)
 template <class P>
 __device__ void run_forward(const ProgDev& prog, const typename P::T* mats, int kt, int nb, int par, unsigned cb,
-	typename P::T* tile, Smem& s, typename P::T* slot, bool negconj_end)
+	typename P::T* tile, Smem& s, typename P::T* slot, bool negconj_end, const int* kinds = nullptr)
 {
 	const int Q = 1 << (kt - 2);
 	for (int p = 0; p < prog.npass; p++)
@@ -471,7 +522,8 @@ __device__ void run_forward(const ProgDev& prog, const typename P::T* mats, int 
 			{
 				const GateRec r = prog.gate[gi];
 				const Gate8<typename P::T> G = load_gate(mats, r.g);
-				gate_forward<P>(tile, r, G, Q, tpar, nullptr, s, nlb);
+				if (kinds) gate_forward_kinds<P>(tile, r, G, kinds[r.g], Q, tpar);
+				else gate_forward<P>(tile, r, G, Q, tpar, nullptr, s, nlb);
 				__syncthreads();
 			}
 			tile_store<P>(tile, kt, s, nlb, slot, negconj_end && p == prog.npass - 1);
@@ -504,7 +556,7 @@ __global__ void __launch_bounds__(256) k_columns(Args<P> a)
 		if (a.dense) dsrc = a.dense + (size_t)(b - a.dense_b0) * S;
 		else
 		{
-			run_forward<P>(a.U, a.um, kt, a.nb, par, cb, tile, s, su, true);
+			run_forward<P>(a.U, a.um, kt, a.nb, par, cb, tile, s, su, true, a.ukind);
 			dsrc = su;
 		}
 		if (a.ucols)
@@ -799,8 +851,62 @@ struct TargetProg
 {
 	int kt = -1, prec = -1;
 	Sched sched;
-	DevBuf pass, gate, mats;
+	DevBuf pass, gate, mats, kinds;
 };
+
+// Exact classification of a 2x2 block (entries row-major); for BK_RI the entries are
+// stored as (c_re, c_im) coefficients of the possibly swapped components of the input:
+// real a -> (a, a), imaginary i b -> (-b, b) with the swap bit set.
+static int classify_block(const mgc* e, unsigned& rot, mgc* stored)
+{
+	auto is = [](mgc z, double re, double im) { return z.re == re && z.im == im; };
+	for (int q = 0; q < 4; q++) stored[q] = e[q];
+	rot = 0;
+	const bool offz = is(e[1], 0, 0) && is(e[2], 0, 0), diagz = is(e[0], 0, 0) && is(e[3], 0, 0);
+	if (offz && is(e[0], 1, 0) && is(e[3], 1, 0)) return BK_ID;
+	if (diagz && is(e[1], 1, 0) && is(e[2], 1, 0)) return BK_SWAP;
+	if (offz && is(e[0], 1, 0) && is(e[3], -1, 0)) return BK_NEG1;
+	if (offz && is(e[0], 1, 0)) return BK_D1;
+	if (offz) return BK_DIAG;
+	if (diagz) return BK_ANTI;
+	bool ri = true;
+	for (int q = 0; q < 4; q++) ri = ri && (e[q].re == 0 || e[q].im == 0);
+	if (!ri) return BK_GEN;
+	for (int q = 0; q < 4; q++)
+	{
+		if (e[q].re == 0 && e[q].im != 0) { rot |= 1u << q; stored[q] = mgc_make(-e[q].im, e[q].im); }
+		else stored[q] = mgc_make(e[q].re, e[q].re);
+	}
+	return BK_RI;
+}
+
+template <class P>
+static int upload_target_mats(const mgg* gates, int ng, DevBuf& buf, DevBuf& kinds)
+{
+	typedef typename P::T T;
+	std::vector<T> h((size_t)std::max(ng, 1) * 8);
+	std::vector<int> k((size_t)std::max(ng, 1));
+	for (int g = 0; g < ng; g++)
+	{
+		mgc sc[4], sk[4];
+		unsigned rc, rk;
+		const int kc = classify_block(gates[g].c, rc, sc), kk = classify_block(gates[g].k, rk, sk);
+		k[g] = kc | (kk << 3) | (int)(rc << 6) | (int)(rk << 10);
+		for (int q = 0; q < 4; q++)
+		{
+			h[(size_t)g * 8 + q] = P::make(sc[q].re, sc[q].im);
+			h[(size_t)g * 8 + 4 + q] = P::make(sk[q].re, sk[q].im);
+		}
+	}
+	int e = buf.alloc(sizeof(T) * h.size());
+	if (!e) e = kinds.alloc(sizeof(int) * k.size());
+	if (e) return e;
+	cudaStream_t st = mgcu_ctx()->stream;
+	MGCU_TRY(cudaMemcpyAsync(buf.p, h.data(), sizeof(T) * h.size(), cudaMemcpyHostToDevice, st));
+	MGCU_TRY(cudaMemcpyAsync(kinds.p, k.data(), sizeof(int) * k.size(), cudaMemcpyHostToDevice, st));
+	MGCU_TRY(cudaStreamSynchronize(st));
+	return 0;
+}
 
 struct mgcu_target
 {
@@ -856,7 +962,7 @@ static int target_prog(mgcu_target* t, int kt, TargetProg*& out)
 		schedule(t->L, kt, t->wires.data(), (int)t->gates.size(), true, tp.sched);
 		int e = upload_sched(tp.sched, tp.pass, tp.gate);
 		if (e) return e;
-		e = upload_mats<P>(t->gates.data(), (int)t->gates.size(), tp.mats);
+		e = upload_target_mats<P>(t->gates.data(), (int)t->gates.size(), tp.mats, tp.kinds);
 		if (e) return e;
 		tp.kt = kt;
 	}
@@ -947,6 +1053,7 @@ static int launch_columns(mgcu_plan* p, long b0, long b1, const typename P::T* d
 		if (e) return e;
 		a.U.pass = tp->pass.as<PassRec>(); a.U.gate = tp->gate.as<GateRec>(); a.U.npass = (int)tp->sched.pass.size();
 		a.um = tp->mats.as<T>();
+		a.ukind = tp->kinds.as<int>();
 	}
 	a.dense = dense; a.dense_b0 = dense_b0;
 	a.b0 = b0; a.b1 = b1;

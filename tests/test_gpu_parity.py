@@ -347,3 +347,68 @@ def test_algebra_on_gpu(lib, oracle):
         z1, b1 = lib.truncated_cg(g, H, radius, 2 * n)
         z2, b2 = oracle.truncated_cg(g, H, radius, 2 * n)
         assert b1 == b2 and udist(z1, z2) < 1e-10
+
+
+def _structured_gates(n, rng):
+    """gates whose blocks are drawn from every structure the target sweep specialises:
+    identity, swap, diag(1,-1), diag(1,a), diagonal, anti-diagonal, real-or-imaginary, general"""
+    def block(kind):
+        z = crandn((2, 2), rng)
+        if kind == 0: return np.eye(2)
+        if kind == 1: return np.array([[0, 1], [1, 0]], complex)
+        if kind == 2: return np.diag([1, -1]).astype(complex)
+        if kind == 3: return np.diag([1, z[1, 1]])
+        if kind == 4: return np.diag([z[0, 0], z[1, 1]])
+        if kind == 5: return np.array([[0, z[0, 1]], [z[1, 0], 0]])
+        if kind == 6:
+            r = rng.standard_normal((2, 2))
+            return np.where(rng.random((2, 2)) < 0.5, r + 0j, 1j * r)
+        return z
+    out = np.zeros((n, 8), complex)
+    for g in range(n):
+        out[g, :4] = block(rng.integers(8)).reshape(4)
+        out[g, 4:] = block(rng.integers(8)).reshape(4)
+    return out
+
+
+@pytest.mark.parametrize("prec,tol", [(mgcu.PREC_FP64, 1e-12), (mgcu.PREC_MIXED, 1e-12), (mgcu.PREC_FP32, 1e-4)])
+@pytest.mark.parametrize("L,tile_bits", [(8, 0), (10, 6)])
+def test_structured_target_blocks_vs_oracle(lib, oracle, prec, tol, L, tile_bits):
+    rng = np.random.default_rng(L + tile_bits)
+    ng = 120
+    gates = _structured_gates(ng, rng)
+    wires = np.array([rng.choice(L, 2, replace=False) for _ in range(ng)], np.int32)
+    nl = 3
+    v = random_gates(nl, rng, unitary=True)
+    perms = brickwall_perms(L, nl, rng)
+    t = lib.target_circuit(gates, wires, L)
+    lib.set_precision(prec)
+    lib.set_option(mgcu.OPT_TILE_BITS, tile_bits)
+    try:
+        rc, f, dv = lib.brickwall_target_and_gradient(lib.mg_target_apply, t, v, perms, L)
+    finally:
+        lib.set_precision(mgcu.PREC_FP64)
+        lib.set_option(mgcu.OPT_TILE_BITS, 0)
+        lib.target_free(t)
+    assert rc == 0
+    f_o, dv_o = oracle.brickwall_target_and_gradient(oracle.Target("circuit", L, gates=gates, wires=wires), v, perms, L)
+    scale = max(1.0, abs(f_o))
+    assert abs(f - f_o) < tol * scale
+    assert np.max(np.abs(dv - dv_o)) < tol * max(1.0, np.max(np.abs(dv_o)))
+
+
+def test_hubbard_target_vs_oracle(lib, oracle):
+    import targets as T
+    rng = np.random.default_rng(6)
+    L = 8
+    g, w, _ = T.hubbard_trotter_circuit(L // 2, 1.0, 4.0, 0.25, 8)
+    v = T.near_identity_brickwall(4, rng)
+    perms = T.brickwall_perms(L, 4)
+    t = lib.target_circuit(g, w, L)
+    try:
+        rc, f, dv, h = lib.brickwall_target_gradient_hessian(lib.mg_target_apply, t, v, perms, L)
+    finally:
+        lib.target_free(t)
+    assert rc == 0
+    f_o, dv_o, h_o = oracle.brickwall_target_gradient_hessian(oracle.Target("circuit", L, gates=g, wires=w), v, perms, L)
+    assert abs(f - f_o) < 1e-12 * abs(f_o) and udist(dv, dv_o) < 1e-11 and udist(h, h_o) < 1e-11
