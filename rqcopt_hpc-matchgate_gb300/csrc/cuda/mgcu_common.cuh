@@ -192,6 +192,11 @@ struct PrecF
 };
 
 // float-float complex sweeps ("mixed"): T = (re_hi, im_hi, re_lo, im_lo)
+// Float-float complex numbers (re_hi, im_hi, re_lo, im_lo).  Results of madd2 / mul /
+// madd2_ri are not renormalised: hi is the rounded sum of the hi products and lo collects
+// the exact product and sum errors and the lo cross terms, so |lo| stays within a few
+// units in the last place of the inputs' magnitude and hi + lo carries about 44
+// significant bits; every consumer uses hi + lo, never hi alone.
 struct PrecX
 {
 	typedef float4 T;
@@ -206,7 +211,7 @@ struct PrecX
 	// a x + b y with every real part summed as a 4-term compensated dot product
 	__device__ static T madd2(T a, T x, T b, T y)
 	{
-		float rh, rl, ih, il, s, t;
+		float rh, rl, ih, il;
 		// real: a.re x.re - a.im x.im + b.re y.re - b.im y.im
 		ff_prod(a.x, a.z, x.x, x.z, rh, rl);
 		ff_acc_prod(rh, rl, -a.y, -a.w, x.y, x.w);
@@ -217,40 +222,31 @@ struct PrecX
 		ff_acc_prod(ih, il, a.y, a.w, x.x, x.z);
 		ff_acc_prod(ih, il, b.x, b.z, y.y, y.w);
 		ff_acc_prod(ih, il, b.y, b.w, y.x, y.z);
-		T r;
-		fast_two_sum(rh, rl, s, t); r.x = s; r.z = t;
-		fast_two_sum(ih, il, s, t); r.y = s; r.w = t;
-		return r;
+		return make_float4(rh, ih, rl, il);
 	}
 	__device__ static T negconj(T a) { return make_float4(-a.x, a.y, -a.z, a.w); }
 	__device__ static T neg(T a) { return make_float4(-a.x, -a.y, -a.z, -a.w); }
 	// a x as two 2-term compensated dot products
 	__device__ static T mul(T a, T x)
 	{
-		float rh, rl, ih, il, s, t;
+		float rh, rl, ih, il;
 		ff_prod(a.x, a.z, x.x, x.z, rh, rl);
 		ff_acc_prod(rh, rl, -a.y, -a.w, x.y, x.w);
 		ff_prod(a.x, a.z, x.y, x.w, ih, il);
 		ff_acc_prod(ih, il, a.y, a.w, x.x, x.z);
-		T r;
-		fast_two_sum(rh, rl, s, t); r.x = s; r.z = t;
-		fast_two_sum(ih, il, s, t); r.y = s; r.w = t;
-		return r;
+		return make_float4(rh, ih, rl, il);
 	}
 	// a x + b y for real-or-imaginary entries (see PrecD::madd2_ri): 2-term dots per part
 	__device__ static T madd2_ri(T a, bool ra, T x, T b, bool rb, T y)
 	{
 		const float xrh = ra ? x.y : x.x, xrl = ra ? x.w : x.z, xih = ra ? x.x : x.y, xil = ra ? x.z : x.w;
 		const float yrh = rb ? y.y : y.x, yrl = rb ? y.w : y.z, yih = rb ? y.x : y.y, yil = rb ? y.z : y.w;
-		float rh, rl, ih, il, s, t;
+		float rh, rl, ih, il;
 		ff_prod(a.x, a.z, xrh, xrl, rh, rl);
 		ff_acc_prod(rh, rl, b.x, b.z, yrh, yrl);
 		ff_prod(a.y, a.w, xih, xil, ih, il);
 		ff_acc_prod(ih, il, b.y, b.w, yih, yil);
-		T r;
-		fast_two_sum(rh, rl, s, t); r.x = s; r.z = t;
-		fast_two_sum(ih, il, s, t); r.y = s; r.w = t;
-		return r;
+		return make_float4(rh, ih, rl, il);
 	}
 	__device__ static Acc acc_zero() { return PrecF::acc_zero(); }
 	__device__ static void acc_mul_add(Acc& s, T d, T x)

@@ -21,12 +21,15 @@
 #include "mgcu_common.cuh"
 
 #include <algorithm>
+#include <array>
+#include <map>
 #include <vector>
 
 namespace {
 
 constexpr int MAXKT = 14;   // at most 2^14 amplitudes per shared-memory tile
 constexpr int MAXNB = 31;   // compact bits (L <= 32)
+constexpr int MAXPM = 128;  // distinct gate matrices per target pass (staged in shared memory)
 
 struct PassRec
 {
@@ -52,11 +55,13 @@ int compact_bit(int L, int q) { return q == L - 1 ? -1 : L - 2 - q; }
 
 // Build the pass schedule of a gate sequence.  reorder = false keeps the sequential
 // order (passes are contiguous runs); reorder = true greedily pulls ready gates (all
-// earlier gates on both wires scheduled) that add the fewest new local bits.
-void schedule(int L, int kt, const int* wires, int ng, bool reorder, Sched& s)
+// earlier gates on both wires scheduled) that add the fewest new local bits.  The
+// lowest `low` compact bits are local in every pass, so that the tile's global reads
+// and writes use whole 32-byte sectors.
+void schedule(int L, int kt, const int* wires, int ng, bool reorder, Sched& s, int low = 3)
 {
 	const int nb = L - 1;
-	const int c0 = std::min(3, kt);
+	const int c0 = std::min(low, kt);
 	s.pass.clear(); s.gate.clear(); s.pass_of.assign(ng, -1);
 
 	std::vector<int> order;
@@ -163,6 +168,18 @@ void schedule(int L, int kt, const int* wires, int ng, bool reorder, Sched& s)
 
 __device__ __forceinline__ unsigned ins0u(unsigned t, int p) { return ((t >> p) << (p + 1)) | (t & ((1u << p) - 1u)); }
 
+// Target gate record, precomputed on the host for a tile size and a block size
+// (all offsets in bytes of the swizzled tile):
+//   m   = { MW, MY, MZ, SCX }: a quartet's w, y, z slots are its x slot XOR MW, MY, MZ;
+//         x itself moves by SCX when the quartet's base has odd parity (gates on the
+//         dropped qubit pair by parity; SCX = 0 otherwise)
+//   h.x = lo | hi << 5 | dpar << 10 | kind word << 13  (lo < hi: the local bits a quartet
+//         spans; dpar: parities of the quartet offsets d1, d2, d4)
+//   h.y = the gate's slot among its pass's matrices, h.z = d1, h.w = d2, d4 = the
+//         offset of quartet 4 (QPT 8)
+// where dk is the swizzled slot offset of quartet t + k * blockDim from quartet t.
+struct TGate { int4 m; int4 h; int d4, pad0, pad1, pad2; };
+
 struct ProgDev
 {
 	const PassRec* pass;
@@ -180,6 +197,10 @@ struct Args
 	const T* wm;               // W gate matrices [ngates][8]: c0..c3, k0..k3
 	const T* um;               // target gate matrices
 	const int* ukind;          // target block kinds (null: every block general)
+	const TGate* utg;          // target gate records (k_target)
+	const int2* upm;           // per target pass: offset into upmats (entries), matrix count
+	const T* upmats;           // per-pass distinct target matrices [8 entries each]
+	unsigned pm_off;           // byte offset of the staged matrices in shared memory
 	int ngates;
 	const T* dense;            // -conj(U e_b) columns, or null (then U is run)
 	long dense_b0;
@@ -200,7 +221,7 @@ struct Args
 	int nplace, mdim;          // mdim = 8 * nblocks
 	double* part_h;            // [grid][mdim][mdim][2]
 	T* sh;                     // per-block slot for placeholder states
-	T* ucols;                  // target-only launch: output columns [b - b0][S]
+	T* ucols;                  // k_target: output columns [b - b0][S]
 };
 
 // shared-memory layout: tile, then the two deposit tables, then reduction scratch
@@ -533,9 +554,250 @@ __device__ void run_forward(const ProgDev& prog, const typename P::T* mats, int 
 }
 
 // ------------------------------------------------------------------------------------
-// stage A: per column -- target, W forward with cache, overlap, W backward
+// target sweep: -conj(U e_b) of a circuit target, one column per block at a time.
+//
+// The tile of this kernel is stored swizzled: local index e lives in slot tsw(e), whose
+// low bits are XORed with two higher bits (16-byte amplitudes: bits 3, 4 -> masks 7, 3;
+// 8-byte amplitudes: bits 4, 5 -> masks 15, 7).  The map is linear over XOR, so a
+// quartet's four slots are one slot XOR three per-gate masks, and eight (sixteen)
+// consecutive threads hit distinct 16-byte (8-byte) bank groups for every pair of gate
+// bits except two.  Gate records are packed (TGate), prefetched one gate ahead, and
+// each thread applies a gate to QPT quartets at once: loads first, then arithmetic,
+// then stores, with the block-kind dispatch outside the quartet batch.
 // ------------------------------------------------------------------------------------
+template <int ES>
+__host__ __device__ __forceinline__ unsigned tsw(unsigned e)
+{
+	return ES == 16 ? (e ^ (((e >> 3) & 1u) * 7u) ^ (((e >> 4) & 1u) * 3u))
+	                : (e ^ (((e >> 4) & 1u) * 15u) ^ (((e >> 5) & 1u) * 7u));
+}
+
+
+template <class P, int QPT>
+__device__ __forceinline__ void tgt_block(char* tb, const unsigned (&x)[QPT], unsigned m0, unsigned m1, int kind, unsigned rot,
+	const typename P::T* m)
+{
+	typedef typename P::T T;
+	T a[QPT], b[QPT];
+	switch (kind)
+	{
+	case BK_ID: return;
+	case BK_SWAP:
+#pragma unroll
+		for (int k = 0; k < QPT; k++) { a[k] = *(T*)(tb + (x[k] ^ m0)); b[k] = *(T*)(tb + (x[k] ^ m1)); }
+#pragma unroll
+		for (int k = 0; k < QPT; k++) { *(T*)(tb + (x[k] ^ m0)) = b[k]; *(T*)(tb + (x[k] ^ m1)) = a[k]; }
+		return;
+	case BK_NEG1:
+#pragma unroll
+		for (int k = 0; k < QPT; k++) b[k] = *(T*)(tb + (x[k] ^ m1));
+#pragma unroll
+		for (int k = 0; k < QPT; k++) *(T*)(tb + (x[k] ^ m1)) = P::neg(b[k]);
+		return;
+	case BK_D1:
+	{
+		const T c3 = m[3];
+#pragma unroll
+		for (int k = 0; k < QPT; k++) b[k] = *(T*)(tb + (x[k] ^ m1));
+#pragma unroll
+		for (int k = 0; k < QPT; k++) *(T*)(tb + (x[k] ^ m1)) = P::mul(c3, b[k]);
+		return;
+	}
+	case BK_DIAG:
+	{
+		const T c0 = m[0], c3 = m[3];
+#pragma unroll
+		for (int k = 0; k < QPT; k++) { a[k] = *(T*)(tb + (x[k] ^ m0)); b[k] = *(T*)(tb + (x[k] ^ m1)); }
+#pragma unroll
+		for (int k = 0; k < QPT; k++) { *(T*)(tb + (x[k] ^ m0)) = P::mul(c0, a[k]); *(T*)(tb + (x[k] ^ m1)) = P::mul(c3, b[k]); }
+		return;
+	}
+	case BK_ANTI:
+	{
+		const T c1 = m[1], c2 = m[2];
+#pragma unroll
+		for (int k = 0; k < QPT; k++) { a[k] = *(T*)(tb + (x[k] ^ m0)); b[k] = *(T*)(tb + (x[k] ^ m1)); }
+#pragma unroll
+		for (int k = 0; k < QPT; k++) { *(T*)(tb + (x[k] ^ m0)) = P::mul(c1, b[k]); *(T*)(tb + (x[k] ^ m1)) = P::mul(c2, a[k]); }
+		return;
+	}
+	case BK_RI:
+	{
+		const T c0 = m[0], c1 = m[1], c2 = m[2], c3 = m[3];
+#pragma unroll
+		for (int k = 0; k < QPT; k++) { a[k] = *(T*)(tb + (x[k] ^ m0)); b[k] = *(T*)(tb + (x[k] ^ m1)); }
+		if (rot == 6u)   // real diagonal, imaginary off-diagonal (hopping terms)
+		{
+#pragma unroll
+			for (int k = 0; k < QPT; k++)
+			{
+				*(T*)(tb + (x[k] ^ m0)) = P::madd2_ri(c0, false, a[k], c1, true, b[k]);
+				*(T*)(tb + (x[k] ^ m1)) = P::madd2_ri(c2, true, a[k], c3, false, b[k]);
+			}
+		}
+		else
+		{
+#pragma unroll
+			for (int k = 0; k < QPT; k++)
+			{
+				*(T*)(tb + (x[k] ^ m0)) = P::madd2_ri(c0, rot & 1, a[k], c1, rot & 2, b[k]);
+				*(T*)(tb + (x[k] ^ m1)) = P::madd2_ri(c2, rot & 4, a[k], c3, rot & 8, b[k]);
+			}
+		}
+		return;
+	}
+	default:
+	{
+		const T c0 = m[0], c1 = m[1], c2 = m[2], c3 = m[3];
+#pragma unroll
+		for (int k = 0; k < QPT; k++) { a[k] = *(T*)(tb + (x[k] ^ m0)); b[k] = *(T*)(tb + (x[k] ^ m1)); }
+#pragma unroll
+		for (int k = 0; k < QPT; k++)
+		{
+			*(T*)(tb + (x[k] ^ m0)) = P::madd2(c0, a[k], c1, b[k]);
+			*(T*)(tb + (x[k] ^ m1)) = P::madd2(c2, a[k], c3, b[k]);
+		}
+	}
+	}
+}
+
+// one target gate on the tile: QPT quartets per thread, q = t + k * blockDim.x
+// (QPT * blockDim.x == number of quartets)
+template <class P, int QPT>
+__device__ __forceinline__ void tgt_gate(char* tb, const TGate& r, const typename P::T* mats, int tpar)
+{
+	constexpr int ES = sizeof(typename P::T);
+	const unsigned MW = r.m.x, MY = r.m.y, MZ = r.m.z, SCX = r.m.w;
+	const int lo = r.h.x & 31, hi = (r.h.x >> 5) & 31;
+	const unsigned dpar = (unsigned)(r.h.x >> 10) & 7u;
+	const unsigned b0 = ins0u(ins0u(threadIdx.x, lo), hi);
+	const unsigned sb0 = tsw<ES>(b0) * ES;
+	const unsigned p0 = (unsigned)(__popc(b0) + tpar) & 1u;
+	const unsigned d1 = r.h.z, d2 = r.h.w, d4 = r.d4;
+	unsigned x[QPT];
+#pragma unroll
+	for (int k = 0; k < QPT; k++)
+	{
+		const unsigned dk = ((k & 1) ? d1 : 0u) ^ ((k & 2) ? d2 : 0u) ^ ((k & 4) ? d4 : 0u);
+		const unsigned pk = p0 ^ (((k & 1) ? dpar : 0u) & 1u) ^ (((k & 2) ? (dpar >> 1) : 0u) & 1u) ^ (((k & 4) ? (dpar >> 2) : 0u) & 1u);
+		x[k] = sb0 ^ dk ^ (pk ? SCX : 0u);
+	}
+	const int kw = r.h.x >> 13;
+	const typename P::T* m = mats + (size_t)r.h.y * 8;
+	tgt_block<P, QPT>(tb, x, 0u, MW, (kw >> 3) & 7, (kw >> 10) & 15, m + 4);
+	tgt_block<P, QPT>(tb, x, MY, MZ, kw & 7, (kw >> 6) & 15, m);
+}
+
+// the same with one quartet per iteration, for tiles whose quartet count is not 4 or 8
+// times the block size
 template <class P>
+__device__ __forceinline__ void tgt_gate_any(char* tb, const TGate& r, const typename P::T* mats, int tpar, unsigned Q)
+{
+	constexpr int ES = sizeof(typename P::T);
+	const unsigned MW = r.m.x, MY = r.m.y, MZ = r.m.z, SCX = r.m.w;
+	const int lo = r.h.x & 31, hi = (r.h.x >> 5) & 31;
+	const int kw = r.h.x >> 13;
+	const typename P::T* m = mats + (size_t)r.h.y * 8;
+	for (unsigned q = threadIdx.x; q < Q; q += blockDim.x)
+	{
+		const unsigned e = ins0u(ins0u(q, lo), hi);
+		const unsigned x[1] = { (tsw<ES>(e) * ES) ^ (((__popc(e) + tpar) & 1) ? SCX : 0u) };
+		tgt_block<P, 1>(tb, x, 0u, MW, (kw >> 3) & 7, (kw >> 10) & 15, m + 4);
+		tgt_block<P, 1>(tb, x, MY, MZ, kw & 7, (kw >> 6) & 15, m);
+	}
+}
+
+// the gates [gbeg, gend) of a pass on one tile, records read one gate ahead
+template <class P, int QPT>
+__device__ __forceinline__ void tgt_gates(char* tb, const TGate* gates, int gbeg, int gend, const typename P::T* mats, int tpar, unsigned Q)
+{
+	if (gbeg >= gend) return;
+	TGate r = gates[gbeg];
+	for (int gi = gbeg; gi < gend; gi++)
+	{
+		const TGate rn = gates[min(gi + 1, gend - 1)];
+		if (QPT > 0) tgt_gate<P, (QPT > 0 ? QPT : 1)>(tb, r, mats, tpar);
+		else tgt_gate_any<P>(tb, r, mats, tpar, Q);
+		__syncthreads();
+		r = rn;
+	}
+}
+
+template <class P>
+__global__ void __launch_bounds__(256, 2) k_target(Args<P> a)
+{
+	typedef typename P::T T;
+	constexpr int ES = sizeof(T);
+	extern __shared__ __align__(16) char smem_raw[];
+	T* tile;
+	Smem s = smem_layout<T>(smem_raw, a.kt, tile);
+	char* tb = reinterpret_cast<char*>(tile);
+	T* pm = reinterpret_cast<T*>(smem_raw + a.pm_off);   // this pass's distinct matrices
+	const int kt = a.kt;
+	const unsigned n = 1u << kt, Q = n >> 2;
+	const int qpt = (Q == 4u * blockDim.x) ? 4 : (Q == 8u * blockDim.x) ? 8 : 0;
+	for (long b = a.b0 + blockIdx.x; b < a.b1; b += gridDim.x)
+	{
+		const int par = __popcll(b) & 1;
+		const unsigned cb = (unsigned)(b >> 1);
+		T* out = a.ucols + (size_t)(b - a.b0) * a.S;
+		for (int p = 0; p < a.U.npass; p++)
+		{
+			const PassRec& pr = a.U.pass[p];
+			__syncthreads();
+			setup_pass(pr, kt, s);
+			{
+				const int2 mp = a.upm[p];
+				for (int i = threadIdx.x; i < mp.y * 8; i += blockDim.x) pm[i] = a.upmats[mp.x + i];
+			}
+			__syncthreads();
+			const bool last = p == a.U.npass - 1;
+			const unsigned ntile = 1u << pr.nnl;
+			for (unsigned tau = 0; tau < ntile; tau++)
+			{
+				const unsigned nlb = nl_base(pr, tau);
+				const int tpar = (__popc(nlb) + par) & 1;
+				if (p == 0)
+					for (unsigned e = threadIdx.x; e < n; e += blockDim.x)
+						tile[tsw<ES>(e)] = (gidx(s, nlb, e) == cb) ? P::make(1.0, 0.0) : P::zero();
+				else
+					for (unsigned e0 = threadIdx.x; e0 < n; e0 += 8 * blockDim.x)
+					{
+						T v[8];   // eight reads in flight
+#pragma unroll
+						for (int k = 0; k < 8; k++)
+						{
+							const unsigned e = e0 + k * blockDim.x;
+							if (e < n) v[k] = out[gidx(s, nlb, e)];
+						}
+#pragma unroll
+						for (int k = 0; k < 8; k++)
+						{
+							const unsigned e = e0 + k * blockDim.x;
+							if (e < n) tile[tsw<ES>(e)] = v[k];
+						}
+					}
+				__syncthreads();
+				if (qpt == 4) tgt_gates<P, 4>(tb, a.utg, pr.gbeg, pr.gend, pm, tpar, Q);
+				else if (qpt == 8) tgt_gates<P, 8>(tb, a.utg, pr.gbeg, pr.gend, pm, tpar, Q);
+				else tgt_gates<P, 0>(tb, a.utg, pr.gbeg, pr.gend, pm, tpar, Q);
+				for (unsigned e = threadIdx.x; e < n; e += blockDim.x)
+				{
+					const T v = tile[tsw<ES>(e)];
+					out[gidx(s, nlb, e)] = last ? P::negconj(v) : v;
+				}
+				__syncthreads();
+			}
+		}
+	}
+}
+
+// ------------------------------------------------------------------------------------
+// stage A: per column -- W forward with cache, overlap, W backward; the target column
+// comes from `dense` (k_target's output, a dense or host target) or, with WithU, from
+// a sweep of the target program inside this kernel
+// ------------------------------------------------------------------------------------
+template <class P, bool WithU>
 __global__ void __launch_bounds__(256) k_columns(Args<P> a)
 {
 	typedef typename P::T T;
@@ -553,19 +815,11 @@ __global__ void __launch_bounds__(256) k_columns(Args<P> a)
 		const int par = __popcll(b) & 1;
 		const unsigned cb = (unsigned)(b >> 1);
 		const T* dsrc;
-		if (a.dense) dsrc = a.dense + (size_t)(b - a.dense_b0) * S;
+		if (!WithU || a.dense) dsrc = a.dense + (size_t)(b - a.dense_b0) * S;
 		else
 		{
 			run_forward<P>(a.U, a.um, kt, a.nb, par, cb, tile, s, su, true, a.ukind);
 			dsrc = su;
-		}
-		if (a.ucols)
-		{
-			// target-only launch: keep -conj(U e_b)
-			T* out = a.ucols + (size_t)(b - a.b0) * S;
-			for (long e = threadIdx.x; e < S; e += blockDim.x) out[e] = su[e];
-			__syncthreads();
-			continue;
 		}
 		const long slot = a.cache_per_column ? (b - a.b0) : blockIdx.x;
 		T* cache = a.cache ? a.cache + (size_t)slot * a.ngates * S : nullptr;
@@ -849,9 +1103,9 @@ int grid_cap(long work, int threads)
 // ======================================================================================
 struct TargetProg
 {
-	int kt = -1, prec = -1;
+	int kt = -1, prec = -1, threads = -1;
 	Sched sched;
-	DevBuf pass, gate, mats, kinds;
+	DevBuf pass, gate, mats, kinds, tg, pm, pmats;
 };
 
 // Exact classification of a 2x2 block (entries row-major); for BK_RI the entries are
@@ -881,11 +1135,11 @@ static int classify_block(const mgc* e, unsigned& rot, mgc* stored)
 }
 
 template <class P>
-static int upload_target_mats(const mgg* gates, int ng, DevBuf& buf, DevBuf& kinds)
+static int upload_target_mats(const mgg* gates, int ng, DevBuf& buf, DevBuf& kinds, std::vector<int>& k)
 {
 	typedef typename P::T T;
 	std::vector<T> h((size_t)std::max(ng, 1) * 8);
-	std::vector<int> k((size_t)std::max(ng, 1));
+	k.assign((size_t)std::max(ng, 1), 0);
 	for (int g = 0; g < ng; g++)
 	{
 		mgc sc[4], sk[4];
@@ -954,17 +1208,126 @@ static int upload_sched(const Sched& s, DevBuf& pass, DevBuf& gate)
 }
 
 template <class P>
-static int target_prog(mgcu_target* t, int kt, TargetProg*& out)
+static int target_prog(mgcu_target* t, int kt, int threads, TargetProg*& out)
 {
 	TargetProg& tp = t->progs[P::kId];
-	if (tp.kt != kt)
+	if (tp.kt != kt || tp.threads != threads)
 	{
-		schedule(t->L, kt, t->wires.data(), (int)t->gates.size(), true, tp.sched);
+		typedef typename P::T T;
+		schedule(t->L, kt, t->wires.data(), (int)t->gates.size(), true, tp.sched, sizeof(T) >= 16 ? 1 : 2);
+		// distinct matrices, then passes split so that each stages at most MAXPM of them
+		const int ngt = (int)t->gates.size();
+		std::vector<int> uid(std::max(ngt, 1), 0);
+		{
+			std::map<std::array<double, 16>, int> seen;
+			for (int g = 0; g < ngt; g++)
+			{
+				std::array<double, 16> key;
+				memcpy(key.data(), &t->gates[g], sizeof(key));
+				auto it = seen.emplace(key, (int)seen.size()).first;
+				uid[g] = it->second;
+			}
+		}
+		std::vector<int> slot(std::max<size_t>(tp.sched.gate.size(), 1), 0);
+		std::vector<int2> pmh;
+		std::vector<int> pm_first;   // first-use matrix per staged slot, all passes
+		{
+			Sched split;
+			split.pass_of = tp.sched.pass_of;
+			split.gate = tp.sched.gate;
+			for (const PassRec& pr : tp.sched.pass)
+			{
+				int gb = pr.gbeg;
+				while (gb < pr.gend || gb == pr.gbeg)
+				{
+					std::map<int, int> loc;
+					const int off = (int)pm_first.size();
+					int ge = gb;
+					for (; ge < pr.gend; ge++)
+					{
+						const int u = uid[tp.sched.gate[ge].g];
+						auto it = loc.find(u);
+						if (it == loc.end())
+						{
+							if ((int)loc.size() == MAXPM) break;
+							it = loc.emplace(u, (int)loc.size()).first;
+							pm_first.push_back(tp.sched.gate[ge].g);
+						}
+						slot[ge] = it->second;
+					}
+					PassRec q = pr;
+					q.gbeg = gb; q.gend = ge;
+					split.pass.push_back(q);
+					pmh.push_back(make_int2(off * 8, (int)loc.size()));
+					if (ge == gb) break;   // empty pass
+					gb = ge;
+				}
+			}
+			tp.sched.pass.swap(split.pass);
+		}
 		int e = upload_sched(tp.sched, tp.pass, tp.gate);
 		if (e) return e;
-		e = upload_target_mats<P>(t->gates.data(), (int)t->gates.size(), tp.mats, tp.kinds);
+		std::vector<int> kw;
+		e = upload_target_mats<P>(t->gates.data(), (int)t->gates.size(), tp.mats, tp.kinds, kw);
 		if (e) return e;
+		// k_target's records; the auxiliary bit of a gate on the dropped qubit is a high
+		// tile bit, away from the swizzle's two conflicting low pairs
+		constexpr unsigned ES = sizeof(typename P::T);
+		auto ins0 = [](unsigned v, int pos) { return ((v >> pos) << (pos + 1)) | (v & ((1u << pos) - 1u)); };
+		std::vector<TGate> tg(std::max<size_t>(tp.sched.gate.size(), 1));
+		memset(tg.data(), 0, sizeof(TGate) * tg.size());
+		for (size_t i = 0; i < tp.sched.gate.size(); i++)
+		{
+			const GateRec& r = tp.sched.gate[i];
+			int pa, pb;
+			if (r.type == 0) { pa = r.la; pb = r.lb; }
+			else
+			{
+				pa = r.type == 1 ? r.la : r.lb;
+				pb = (pa == kt - 1) ? kt - 2 : kt - 1;
+			}
+			const int lo = std::min(pa, pb), hi = std::max(pa, pb);
+			const unsigned SA = tsw<ES>(1u << pa) * ES, SB = tsw<ES>(1u << pb) * ES;
+			TGate& o = tg[i];
+			o.m.x = (int)(r.type == 0 ? (SA ^ SB) : SA);
+			o.m.y = (int)(r.type == 2 ? (SA ^ SB) : SB);
+			o.m.z = (int)(r.type == 0 ? SA : (r.type == 1 ? (SA ^ SB) : SB));
+			o.m.w = (int)(r.type == 0 ? 0u : SB);
+			unsigned d[3], dpar = 0;
+			for (int k = 0; k < 3; k++)
+			{
+				const unsigned e = ins0(ins0((unsigned)threads << k, lo), hi);
+				d[k] = tsw<ES>(e) * ES;
+				dpar |= (unsigned)(__builtin_popcount(e) & 1) << k;
+			}
+			o.h.x = lo | hi << 5 | (int)(dpar << 10) | kw[r.g] << 13;
+			o.h.y = slot[i];
+			o.h.z = (int)d[0]; o.h.w = (int)d[1]; o.d4 = (int)d[2];
+		}
+		e = tp.tg.alloc(sizeof(TGate) * tg.size());
+		if (e) return e;
+		MGCU_TRY(cudaMemcpy(tp.tg.p, tg.data(), sizeof(TGate) * tg.size(), cudaMemcpyHostToDevice));
+		// staged matrices: the classified entries of each slot's first gate
+		std::vector<T> hm(std::max<size_t>(pm_first.size(), 1) * 8);
+		for (size_t i = 0; i < pm_first.size(); i++)
+		{
+			mgc sc[4], sk[4];
+			unsigned rc, rk;
+			classify_block(t->gates[pm_first[i]].c, rc, sc);
+			classify_block(t->gates[pm_first[i]].k, rk, sk);
+			for (int q = 0; q < 4; q++)
+			{
+				hm[i * 8 + q] = P::make(sc[q].re, sc[q].im);
+				hm[i * 8 + 4 + q] = P::make(sk[q].re, sk[q].im);
+			}
+		}
+		e = tp.pmats.alloc(sizeof(T) * hm.size());
+		if (!e) e = tp.pm.alloc(sizeof(int2) * std::max<size_t>(pmh.size(), 1));
+		if (e) return e;
+		MGCU_TRY(cudaMemcpy(tp.pmats.p, hm.data(), sizeof(T) * hm.size(), cudaMemcpyHostToDevice));
+		MGCU_TRY(cudaMemcpy(tp.pm.p, pmh.data(), sizeof(int2) * pmh.size(), cudaMemcpyHostToDevice));
 		tp.kt = kt;
+		tp.threads = threads;
 	}
 	out = &tp;
 	return 0;
@@ -1021,7 +1384,8 @@ struct mgcu_plan
 	mgcu_plan_desc d;
 	std::vector<int> wires, block, place;
 	std::vector<double> place_w;
-	int L, nb, kt, threads, grid_a, grid_b, prec;
+	int L, nb, kt, threads, grid_a, grid_b, grid_t, prec;
+	size_t smem_t;                 // k_target: smem plus MAXPM staged matrices
 	long S;
 	size_t tsize;
 	size_t smem;
@@ -1035,8 +1399,35 @@ struct mgcu_plan
 
 static size_t prec_tsize(int prec) { return prec == MG_PREC_FP32_ID ? 8 : 16; }
 
+// -conj(U e_b) of a circuit target for b in [b0, b1) into out[b - b0]
 template <class P>
-static int launch_columns(mgcu_plan* p, long b0, long b1, const typename P::T* dense, long dense_b0, typename P::T* ucols)
+static int launch_target(mgcu_plan* p, long b0, long b1, typename P::T* out)
+{
+	typedef typename P::T T;
+	MgcuContext* c = mgcu_ctx();
+	Args<P> a;
+	memset(&a, 0, sizeof(a));
+	a.L = p->L; a.nb = p->nb; a.kt = p->kt; a.S = p->S;
+	TargetProg* tp = nullptr;
+	int e = target_prog<P>(p->d.target, p->kt, p->threads, tp);
+	if (e) return e;
+	a.U.pass = tp->pass.as<PassRec>(); a.U.gate = tp->gate.as<GateRec>(); a.U.npass = (int)tp->sched.pass.size();
+	a.um = tp->mats.as<T>();
+	a.utg = tp->tg.as<TGate>();
+	a.upm = tp->pm.as<int2>();
+	a.upmats = tp->pmats.as<T>();
+	a.pm_off = (unsigned)p->smem;
+	a.b0 = b0; a.b1 = b1;
+	a.ucols = out;
+	const int grid = (int)std::min<long>(p->grid_t, b1 - b0);
+	k_target<P><<<grid, p->threads, p->smem_t, c->stream>>>(a);
+	MGCU_LAUNCHED();
+	return 0;
+}
+
+// f, gradients (and Hessian items) for columns [b0, b1) whose -conj(U e_b) are in dense
+template <class P>
+static int launch_columns(mgcu_plan* p, long b0, long b1, const typename P::T* dense, long dense_b0)
 {
 	typedef typename P::T T;
 	MgcuContext* c = mgcu_ctx();
@@ -1046,15 +1437,6 @@ static int launch_columns(mgcu_plan* p, long b0, long b1, const typename P::T* d
 	a.W.pass = p->d_pass.as<PassRec>(); a.W.gate = p->d_gate.as<GateRec>(); a.W.npass = (int)p->ws.pass.size();
 	a.wm = p->d_mats.as<T>();
 	a.ngates = p->d.ngates;
-	if (!dense)
-	{
-		TargetProg* tp = nullptr;
-		int e = target_prog<P>(p->d.target, p->kt, tp);
-		if (e) return e;
-		a.U.pass = tp->pass.as<PassRec>(); a.U.gate = tp->gate.as<GateRec>(); a.U.npass = (int)tp->sched.pass.size();
-		a.um = tp->mats.as<T>();
-		a.ukind = tp->kinds.as<int>();
-	}
 	a.dense = dense; a.dense_b0 = dense_b0;
 	a.b0 = b0; a.b1 = b1;
 	a.su = p->su.as<T>(); a.sw = p->sw.as<T>();
@@ -1064,13 +1446,12 @@ static int launch_columns(mgcu_plan* p, long b0, long b1, const typename P::T* d
 	a.want_grad = p->d.want_grad || p->d.want_hess;
 	a.part_f = p->part_f.as<double>();
 	a.part_g = p->part_g.as<double>();
-	a.ucols = ucols;
-	if (!a.want_grad && !ucols) a.cache = nullptr;
+	if (!a.want_grad) a.cache = nullptr;
 	const long ncols = b1 - b0;
 	const int grid = (int)std::min<long>(p->grid_a, ncols);
-	k_columns<P><<<grid, p->threads, p->smem, c->stream>>>(a);
+	k_columns<P, false><<<grid, p->threads, p->smem, c->stream>>>(a);
 	MGCU_LAUNCHED();
-	if (p->d.want_hess && !ucols)
+	if (p->d.want_hess)
 	{
 		a.place = p->d_place.as<int>(); a.place_w = p->d_placew.as<double>(); a.pass_of = p->d_pass_of.as<int>();
 		a.block = p->d_block.as<int>(); a.nplace = p->d.nplace; a.mdim = 8 * p->d.nblocks;
@@ -1087,18 +1468,21 @@ template <class P>
 static int set_smem_attr()
 {
 	MgcuContext* c = mgcu_ctx();
-	MGCU_TRY(cudaFuncSetAttribute(k_columns<P>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)std::min<size_t>(c->smem_optin, 227 * 1024)));
+	MGCU_TRY(cudaFuncSetAttribute(k_columns<P, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)std::min<size_t>(c->smem_optin, 227 * 1024)));
+	MGCU_TRY(cudaFuncSetAttribute(k_target<P>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)std::min<size_t>(c->smem_optin, 227 * 1024)));
 	MGCU_TRY(cudaFuncSetAttribute(k_hessian<P>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)std::min<size_t>(c->smem_optin, 227 * 1024)));
 	return 0;
 }
 
 template <class P>
-static int occupancy(int threads, size_t smem, int& per_sm)
+static int occupancy(int threads, size_t smem, size_t smem_t, int& per_sm, int& per_sm_target)
 {
-	int n1 = 0, n2 = 0;
-	MGCU_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n1, k_columns<P>, threads, smem));
+	int n1 = 0, n2 = 0, n3 = 0;
+	MGCU_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n1, k_columns<P, false>, threads, smem));
 	MGCU_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n2, k_hessian<P>, threads, smem));
+	MGCU_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n3, k_target<P>, threads, smem_t));
 	per_sm = std::max(1, std::min(n1, n2));
+	per_sm_target = std::max(1, n3);
 	return 0;
 }
 
@@ -1145,14 +1529,16 @@ extern "C" mgcu_plan* mgcu_plan_create(const mgcu_plan_desc* d)
 	const long opt_thr = mgcu_option(MG_OPT_THREADS_ID);
 	if (opt_thr > 0) threads = (int)std::max(32L, std::min(256L, (opt_thr / 32) * 32));
 	p->threads = threads;
-	p->smem = ((size_t)1 << p->kt) * p->tsize + 2 * 128 * sizeof(unsigned) + (size_t)(threads / 32) * 16 * sizeof(double);
+	// tile, deposit tables, reduction scratch (also k_target's 16 staged gate entries)
+	p->smem = ((size_t)1 << p->kt) * p->tsize + 2 * 128 * sizeof(unsigned) + std::max<size_t>((size_t)(threads / 32) * 16 * sizeof(double), 16 * 16);
 
 	schedule(p->L, p->kt, p->wires.data(), d->ngates, false, p->ws);
 
-	int per_sm = 1, e = 0;
-	if (p->prec == MG_PREC_FP64_ID) { e = set_smem_attr<PrecD>(); if (!e) e = occupancy<PrecD>(threads, p->smem, per_sm); }
-	else if (p->prec == MG_PREC_FP32_ID) { e = set_smem_attr<PrecF>(); if (!e) e = occupancy<PrecF>(threads, p->smem, per_sm); }
-	else { e = set_smem_attr<PrecX>(); if (!e) e = occupancy<PrecX>(threads, p->smem, per_sm); }
+	p->smem_t = p->smem + (size_t)MAXPM * 8 * p->tsize;
+	int per_sm = 1, per_sm_t = 1, e = 0;
+	if (p->prec == MG_PREC_FP64_ID) { e = set_smem_attr<PrecD>(); if (!e) e = occupancy<PrecD>(threads, p->smem, p->smem_t, per_sm, per_sm_t); }
+	else if (p->prec == MG_PREC_FP32_ID) { e = set_smem_attr<PrecF>(); if (!e) e = occupancy<PrecF>(threads, p->smem, p->smem_t, per_sm, per_sm_t); }
+	else { e = set_smem_attr<PrecX>(); if (!e) e = occupancy<PrecX>(threads, p->smem, p->smem_t, per_sm, per_sm_t); }
 	if (e) { delete p; return nullptr; }
 	const long opt_cps = mgcu_option(MG_OPT_CTAS_PER_SM_ID);
 	if (opt_cps > 0) per_sm = (int)std::min<long>(per_sm, opt_cps);
@@ -1170,11 +1556,12 @@ extern "C" mgcu_plan* mgcu_plan_create(const mgcu_plan_desc* d)
 	grid = std::min(grid, ncols_total);
 	p->grid_a = (int)grid;
 	p->grid_b = (int)((long)c->nsm * per_sm);
+	p->grid_t = (int)((long)c->nsm * (opt_cps > 0 ? std::min<long>(per_sm_t, opt_cps) : per_sm_t));
 
-	// columns per chunk: Hessian caches per column (<= 16 GB) or staged target columns (<= 2 GB)
+	// columns per chunk: Hessian caches per column (<= 16 GB) or staged target columns (<= 8 GB)
 	long chunk = ncols_total;
 	if (d->want_hess) chunk = std::max(1L, std::min(chunk, (long)((16ull << 30) / (2ull * ng * col_bytes))));
-	if (!d->target || d->target->kind == 1) chunk = std::max(1L, std::min(chunk, (long)((2ull << 30) / (col_bytes + (size_t)p->S * 16))));
+	chunk = std::max(1L, std::min(chunk, (long)((8ull << 30) / (col_bytes + (size_t)p->S * 16))));
 	const long opt_chunk = mgcu_option(MG_OPT_CHUNK_COLUMNS_ID);
 	if (opt_chunk > 0) chunk = std::min(chunk, opt_chunk);
 	p->chunk = chunk;
@@ -1197,7 +1584,7 @@ extern "C" mgcu_plan* mgcu_plan_create(const mgcu_plan_desc* d)
 	if (!e && d->want_hess) e = p->out_h.alloc(sizeof(double) * 2 * (size_t)mdim * mdim);
 	if (!e) e = p->d_block.alloc(sizeof(int) * ng);
 	if (!e) e = p->d_pass_of.alloc(sizeof(int) * ng);
-	if (!e && (!d->target || d->target->kind == 1)) e = p->cols.alloc(col_bytes * chunk);
+	if (!e) e = p->cols.alloc(col_bytes * chunk);
 	if (!e && !d->target) e = p->cols64.alloc((size_t)p->S * 16 * chunk);
 	if (!e && d->want_hess) e = p->d_place.alloc(sizeof(int) * std::max(d->nplace, 1));
 	if (!e && d->want_hess) e = p->d_placew.alloc(sizeof(double) * std::max<size_t>((size_t)d->nplace * ng, 1));
@@ -1268,14 +1655,20 @@ static int plan_columns_t(mgcu_plan* p, long b0, long b1, const mgc* host_cols)
 				const long N = 1L << p->L;
 				int e = t->res_cols[id].alloc((size_t)N * p->S * sizeof(T));
 				if (e) return e;
-				e = launch_columns<P>(p, 0, N, nullptr, 0, t->res_cols[id].as<T>());
+				e = launch_target<P>(p, 0, N, t->res_cols[id].as<T>());
 				if (e) return e;
 				t->res_valid[id] = true; t->res_kt[id] = p->kt;
 			}
 			dense = t->res_cols[id].as<T>();
 			dense_b0 = 0;
 		}
-		int e = launch_columns<P>(p, c0, c1, dense, dense_b0, nullptr);
+		else
+		{
+			int e = launch_target<P>(p, c0, c1, p->cols.as<T>());
+			if (e) return e;
+			dense = p->cols.as<T>();
+		}
+		int e = launch_columns<P>(p, c0, c1, dense, dense_b0);
 		if (e) return e;
 	}
 	return 0;
@@ -1520,7 +1913,7 @@ extern "C" int mg_noalloc_brickwall_target_and_gradient(const void* ugates, int 
 		a.want_grad = 1;
 		a.part_f = reinterpret_cast<double*>(base + NA_PART_F);
 		a.part_g = reinterpret_cast<double*>(base + NA_PART_G);
-		k_columns<PrecD><<<grid, threads, smem, st>>>(a);
+		k_columns<PrecD, true><<<grid, threads, smem, st>>>(a);
 		mgcu_count_launch();
 		NA_TRY(cudaGetLastError());
 		k_sum_parts<<<1, 32, 0, st>>>(a.part_f, grid, 2, reinterpret_cast<double*>(base + NA_OUT_F));

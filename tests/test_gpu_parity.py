@@ -412,3 +412,42 @@ def test_hubbard_target_vs_oracle(lib, oracle):
     assert rc == 0
     f_o, dv_o, h_o = oracle.brickwall_target_gradient_hessian(oracle.Target("circuit", L, gates=g, wires=w), v, perms, L)
     assert abs(f - f_o) < 1e-12 * abs(f_o) and udist(dv, dv_o) < 1e-11 and udist(h, h_o) < 1e-11
+
+
+@pytest.mark.parametrize("L,tile_bits,threads,prec", [(10, 0, 0, mgcu.PREC_FP64), (12, 0, 0, mgcu.PREC_MIXED),
+                                                      (12, 9, 0, mgcu.PREC_FP64), (14, 12, 0, mgcu.PREC_MIXED),
+                                                      (14, 12, 128, mgcu.PREC_FP64), (14, 10, 0, mgcu.PREC_FP32),
+                                                      (14, 0, 0, mgcu.PREC_FP32), (14, 13, 0, mgcu.PREC_MIXED)])
+def test_target_sweep_tiles_vs_oracle(lib, oracle, L, tile_bits, threads, prec):
+    """the target-sweep kernel with 1, 2, 4 and 8 quartets per thread, one or several
+    tiles per pass and structured and general gates (also on the dropped qubit), against
+    the oracle"""
+    rng = np.random.default_rng(100 + L + tile_bits + threads)
+    ng = 150
+    gates = np.concatenate([_structured_gates(ng // 2, rng), random_gates(ng - ng // 2, rng, unitary=True)])
+    rng.shuffle(gates)
+    wires = np.array([rng.choice(L, 2, replace=False) for _ in range(ng)], np.int32)
+    for i in range(0, ng, 7):
+        wires[i] = (rng.integers(L - 1), L - 1)
+        if i + 3 < ng:
+            wires[i + 3] = (L - 1, rng.integers(L - 1))
+    nl = 3
+    v = random_gates(nl, rng, unitary=True)
+    perms = brickwall_perms(L, nl, rng)
+    cols = (0, 96)
+    t = lib.target_circuit(gates, wires, L)
+    lib.set_precision(prec)
+    lib.set_option(mgcu.OPT_TILE_BITS, tile_bits)
+    lib.set_option(mgcu.OPT_THREADS, threads)
+    try:
+        rc, f, dv = lib.brickwall_columns(lib.mg_target_apply, t, v, perms, L, *cols)
+    finally:
+        lib.set_option(mgcu.OPT_TILE_BITS, 0)
+        lib.set_option(mgcu.OPT_THREADS, 0)
+        lib.set_precision(mgcu.PREC_FP64)
+        lib.target_free(t)
+    assert rc == 0
+    tol = 1e-4 if prec == mgcu.PREC_FP32 else 1e-12
+    f_o, dv_o = oracle.brickwall_target_and_gradient(oracle.Target("circuit", L, gates=gates, wires=wires), v, perms, L, col_range=cols)
+    sf, sg = max(1.0, abs(f_o)), max(1.0, np.max(np.abs(dv_o)))
+    assert abs(f - f_o) < tol * sf and np.max(np.abs(dv - dv_o)) < tol * sg
