@@ -47,6 +47,8 @@ def parse():
     ap.add_argument("--fp64-columns", type=int, default=2048, help="column sample for the FP64 comparison")
     ap.add_argument("--cpu-seconds", type=float, default=15.0, help="budget of the CPU baseline sample")
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--profile-columns", type=int, default=0,
+                    help="small case for ncu: one evaluation over this many columns, no timing, then exit")
     return ap.parse_args()
 
 
@@ -86,6 +88,13 @@ def workload(L, nlayers, nsteps, seed=3):
     v = T.near_identity_brickwall(nlayers, rng)
     perms = T.brickwall_perms(L, nlayers)
     return g, w, v, perms
+
+
+# DRAM bytes (read + write) of the target-sweep kernel per basis column, from the ncu capture
+# summarised in profiles/k_target_mixed_hubbard_L16.md (608 columns, L=16, mixed); the
+# kernel's traffic is its output columns plus tile round trips that miss L2, both
+# proportional to the number of columns, so per-launch traffic = this x columns per launch
+TARGET_DRAM_BYTES_PER_COLUMN = {16: None}
 
 
 def alg_flops(L, gu, gw, ncols):
@@ -203,6 +212,14 @@ def run_gb300(a):
 
     target = lib.target_circuit(g, w, L)
     lib.set_precision(prec)
+    if a.profile_columns:
+        lib.brickwall_columns(lib.mg_target_apply, target, v, perms, L, 0, min(304, a.profile_columns))
+        rc, f, dv = lib.brickwall_columns(lib.mg_target_apply, target, v, perms, L, 0, a.profile_columns)
+        assert rc == 0, lib.last_error()
+        lib.target_free(target)
+        if rank == 0:
+            print(json.dumps({"profile_columns": a.profile_columns, "L": L, "precision": a.precision, "f": [f.real, f.imag]}))
+        return
     plan = lib.plan_brickwall(lib.mg_target_apply, target, v, perms, L, mgcu.EVAL_GRADIENT)
     for _ in range(a.warmup):
         assert lib.lib.mg_plan_run(mgcu.P(plan)) == 0, lib.last_error()
@@ -213,6 +230,7 @@ def run_gb300(a):
     total_ms = lib.lib.mg_plan_time_ms(mgcu.P(plan), a.steps, 1)
     launches = lib.launch_count() - n0
     clk = clocks.stop()
+    tk_ms, tk_n = lib.plan_target_kernel_ms(plan)
     dist.barrier()
     assert total_ms > 0, lib.last_error()
     f_dev, dv_dev, _, gvec_dev, _ = lib.plan_results(plan, nl, grad=True, proj=True)
@@ -249,7 +267,14 @@ def run_gb300(a):
     rel_g = float(np.linalg.norm(dvx - dv64) / np.linalg.norm(dv64))
 
     flops = alg_flops(L, gu, gw, ncols)
-    achieved = flops / (ms_per_step / 1e3) / 1e12
+    achieved_step = flops / (ms_per_step / 1e3) / 1e12
+    # dominant kernel: the target sweep (k_target), timed by CUDA events around each launch
+    cols_per_launch = ncols * a.steps / tk_n
+    tk_flops = float(cols_per_launch) * (1 << (L - 1)) * 14 * gu
+    tk_avg_s = tk_ms / 1e3 / tk_n
+    achieved = tk_flops / tk_avg_s / 1e12
+    bpc = TARGET_DRAM_BYTES_PER_COLUMN.get(L) if a.precision == "mixed" else None
+    traffic = bpc * cols_per_launch if bpc else None
     out = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": a.steps, "warmup": a.warmup,
         "ms_per_step": ms_per_step, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
@@ -266,9 +291,16 @@ def run_gb300(a):
         "e2e": {"value": world * a.steps / e2e_s, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
                 "timer": "host clock around matchgate_brickwall_unitary_target_and_projected_gradient (synchronous C call)"},
         "roofline": {"bound": "fp32", "achieved": achieved, "peak": fp32_peak / 1e3, "unit": "TFLOP/s",
-                     "frac": achieved / (fp32_peak / 1e3), "traffic": None,
-                     "achieved_is": "algorithmic complex-arithmetic flops (parity sector) per second",
-                     "peak_source": "FP32 FMA microkernel of this library, measured in this run",
+                     "frac": achieved / (fp32_peak / 1e3), "traffic": traffic,
+                     "kernel": "k_target (target sweep)", "kernel_launches": tk_n,
+                     "kernel_ms_per_launch": tk_avg_s * 1e3, "kernel_share_of_step": tk_ms / total_ms,
+                     "columns_per_launch": cols_per_launch,
+                     "achieved_is": "algorithmic complex-arithmetic flops of the target sweep (14 per parity-sector "
+                                    "amplitude and gate) per second of k_target",
+                     "step_achieved": achieved_step,
+                     "peak_source": "FP32 FMA microkernel of this library, measured in this run "
+                                    "(MEASURED_PEAKS.json holds HBM and bf16 tensor peaks only)",
+                     "traffic_source": "ncu dram__bytes_read+write per column, profiles/k_target_mixed_hubbard_L16.md, x columns per launch",
                      "fp64_peak_tflops": fp64_peak / 1e3},
         "fp64_gpu": {"value": fp64_value, "unit": UNIT, "sample_columns": c, "extrapolated_from_sample": True,
                      "speedup_of_timed_precision": value / world / fp64_value},

@@ -29,8 +29,11 @@ int mg_get_precision(void);
 /* Tuning options (0 = automatic).  TILE_BITS: log2 of amplitudes per shared-memory
  * tile; THREADS: threads per block; CHUNK_COLUMNS: basis columns per batch when
  * columns are materialised from a host map or a Hessian is requested;
- * CTAS_PER_SM: resident blocks per SM for the persistent grid. */
-enum { MG_OPT_TILE_BITS = 1, MG_OPT_THREADS = 2, MG_OPT_CHUNK_COLUMNS = 3, MG_OPT_CTAS_PER_SM = 4 };
+ * CTAS_PER_SM: resident blocks per SM for the persistent grid; TARGET_TILE_BITS and
+ * TARGET_THREADS: the same two for the sweep of a GPU circuit target (default: TILE_BITS
+ * and its block size; at most 2^13 amplitudes of 16 B and 512 threads). */
+enum { MG_OPT_TILE_BITS = 1, MG_OPT_THREADS = 2, MG_OPT_CHUNK_COLUMNS = 3, MG_OPT_CTAS_PER_SM = 4,
+       MG_OPT_TARGET_TILE_BITS = 5, MG_OPT_TARGET_THREADS = 6 };
 int mg_set_option(int option, long value);
 long mg_get_option(int option);
 
@@ -98,6 +101,9 @@ void mg_plan_free(mg_plan* plan);
  * library's stream; when flush_l2 != 0 a buffer larger than L2 is written between
  * runs, outside the timed intervals.  Returns the summed milliseconds (< 0 on error). */
 double mg_plan_time_ms(mg_plan* plan, int steps, int flush_l2);
+/* The target-sweep kernel launches inside the last mg_plan_time_ms call (circuit
+ * targets): their number and summed duration from CUDA events around each launch. */
+int mg_plan_target_kernel_ms(mg_plan* plan, double* ms, long* launches);
 /* Number of kernels this library has launched since it was loaded. */
 long mg_launch_count(void);
 /* Peak FP32 FMA rate of this GPU, measured by a dependent-FMA kernel of this library

@@ -122,6 +122,12 @@ struct PrecD
 	}
 	__device__ static T negconj(T a) { return make_double2(-a.x, a.y); }
 	__device__ static T neg(T a) { return make_double2(-a.x, -a.y); }
+	// a with its sign flipped when s == 1 (bit operations, no arithmetic)
+	__device__ static T negif(T a, unsigned s)
+	{
+		const long long m = (long long)s << 63;
+		return make_double2(__longlong_as_double(__double_as_longlong(a.x) ^ m), __longlong_as_double(__double_as_longlong(a.y) ^ m));
+	}
 	__device__ static T mul(T a, T x) { return make_double2(fma(a.x, x.x, -a.y * x.y), fma(a.x, x.y, a.y * x.x)); }
 	// a x + b y for entries that are real or imaginary: a = (c_re, c_im) with c_re, c_im the
 	// coefficients of the (possibly swapped) components of x; swap when the entry is imaginary
@@ -164,6 +170,11 @@ struct PrecF
 	}
 	__device__ static T negconj(T a) { return make_float2(-a.x, a.y); }
 	__device__ static T neg(T a) { return make_float2(-a.x, -a.y); }
+	__device__ static T negif(T a, unsigned s)
+	{
+		const unsigned m = s << 31;
+		return make_float2(__uint_as_float(__float_as_uint(a.x) ^ m), __uint_as_float(__float_as_uint(a.y) ^ m));
+	}
 	__device__ static T mul(T a, T x) { return make_float2(fmaf(a.x, x.x, -a.y * x.y), fmaf(a.x, x.y, a.y * x.x)); }
 	__device__ static T madd2_ri(T a, bool ra, T x, T b, bool rb, T y)
 	{
@@ -226,6 +237,12 @@ struct PrecX
 	}
 	__device__ static T negconj(T a) { return make_float4(-a.x, a.y, -a.z, a.w); }
 	__device__ static T neg(T a) { return make_float4(-a.x, -a.y, -a.z, -a.w); }
+	__device__ static T negif(T a, unsigned s)
+	{
+		const unsigned m = s << 31;
+		return make_float4(__uint_as_float(__float_as_uint(a.x) ^ m), __uint_as_float(__float_as_uint(a.y) ^ m),
+			__uint_as_float(__float_as_uint(a.z) ^ m), __uint_as_float(__float_as_uint(a.w) ^ m));
+	}
 	// a x as two 2-term compensated dot products
 	__device__ static T mul(T a, T x)
 	{

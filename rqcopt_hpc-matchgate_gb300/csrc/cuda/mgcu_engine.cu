@@ -57,8 +57,10 @@ int compact_bit(int L, int q) { return q == L - 1 ? -1 : L - 2 - q; }
 // order (passes are contiguous runs); reorder = true greedily pulls ready gates (all
 // earlier gates on both wires scheduled) that add the fewest new local bits.  The
 // lowest `low` compact bits are local in every pass, so that the tile's global reads
-// and writes use whole 32-byte sectors.
-void schedule(int L, int kt, const int* wires, int ng, bool reorder, Sched& s, int low = 3)
+// and writes use whole 32-byte sectors.  masks (optional, reorder only): per gate the
+// wires of its Jordan-Wigner string; the gate keeps its order relative to every gate
+// acting on one of them (its local bits are still its two wires only).
+void schedule(int L, int kt, const int* wires, int ng, bool reorder, Sched& s, int low = 3, const unsigned* masks = nullptr)
 {
 	const int nb = L - 1;
 	const int c0 = std::min(low, kt);
@@ -96,7 +98,14 @@ void schedule(int L, int kt, const int* wires, int ng, bool reorder, Sched& s, i
 	else
 	{
 		std::vector<std::vector<int>> onq(L);
-		for (int g = 0; g < ng; g++) { onq[wires[2 * g]].push_back(g); onq[wires[2 * g + 1]].push_back(g); }
+		auto wset = [&](int g) {
+			unsigned m = (1u << wires[2 * g]) | (1u << wires[2 * g + 1]);
+			if (masks) m |= masks[g];
+			return m;
+		};
+		for (int g = 0; g < ng; g++)
+			for (int q = 0; q < L; q++)
+				if (wset(g) & (1u << q)) onq[q].push_back(g);
 		std::vector<size_t> fr(L, 0);
 		int done = 0;
 		while (done < ng || passes_gates.empty())
@@ -110,8 +119,11 @@ void schedule(int L, int kt, const int* wires, int ng, bool reorder, Sched& s, i
 				{
 					if (fr[q] >= onq[q].size()) continue;
 					const int g = onq[q][fr[q]];
-					const int q2 = (wires[2 * g] == q) ? wires[2 * g + 1] : wires[2 * g];
-					if (fr[q2] >= onq[q2].size() || onq[q2][fr[q2]] != g) continue;
+					const unsigned ws = wset(g);
+					bool ready = true;
+					for (int q2 = 0; q2 < L && ready; q2++)
+						if ((ws & (1u << q2)) && (fr[q2] >= onq[q2].size() || onq[q2][fr[q2]] != g)) ready = false;
+					if (!ready) continue;
 					const unsigned m = bits_of(g);
 					const int nw = __builtin_popcount(m & ~cur);
 					if (__builtin_popcount(cur | m) > kt) continue;
@@ -119,7 +131,8 @@ void schedule(int L, int kt, const int* wires, int ng, bool reorder, Sched& s, i
 				}
 				if (best < 0) break;
 				cur |= bits_of(best);
-				fr[wires[2 * best]]++; fr[wires[2 * best + 1]]++;
+				for (int q2 = 0; q2 < L; q2++)
+					if (wset(best) & (1u << q2)) fr[q2]++;
 				pg.push_back(best);
 				done++;
 			}
@@ -177,8 +190,13 @@ __device__ __forceinline__ unsigned ins0u(unsigned t, int p) { return ((t >> p) 
 //         spans; dpar: parities of the quartet offsets d1, d2, d4)
 //   h.y = the gate's slot among its pass's matrices, h.z = d1, h.w = d2, d4 = the
 //         offset of quartet 4 (QPT 8)
-// where dk is the swizzled slot offset of quartet t + k * blockDim from quartet t.
-struct TGate { int4 m; int4 h; int d4, pad0, pad1, pad2; };
+//   sl  = Jordan-Wigner string of the gate: local bits | dropped-qubit flag << 16 |
+//         string parities of d1, d2, d4 << 17;  snl = its nonlocal compact bits
+// where dk is the swizzled slot offset of quartet t + k * blockDim from quartet t.  A
+// gate with a string has its off-diagonal entries negated on amplitudes whose string
+// bits have odd parity (a gate conjugated by the controlled-Z of a removed fermionic
+// swap).
+struct TGate { int4 m; int4 h; int d4, sl, snl, pad; };
 
 struct ProgDev
 {
@@ -573,9 +591,11 @@ __host__ __device__ __forceinline__ unsigned tsw(unsigned e)
 }
 
 
-template <class P, int QPT>
+// one 2x2 block on QPT pairs (slots x ^ m0, x ^ m1); SG: off-diagonal entries negated
+// on the pairs with sg[k] == 1 (implemented by negating the off-diagonal inputs)
+template <class P, int QPT, bool SG>
 __device__ __forceinline__ void tgt_block(char* tb, const unsigned (&x)[QPT], unsigned m0, unsigned m1, int kind, unsigned rot,
-	const typename P::T* m)
+	const typename P::T* m, const unsigned (&sg)[QPT])
 {
 	typedef typename P::T T;
 	T a[QPT], b[QPT];
@@ -586,7 +606,11 @@ __device__ __forceinline__ void tgt_block(char* tb, const unsigned (&x)[QPT], un
 #pragma unroll
 		for (int k = 0; k < QPT; k++) { a[k] = *(T*)(tb + (x[k] ^ m0)); b[k] = *(T*)(tb + (x[k] ^ m1)); }
 #pragma unroll
-		for (int k = 0; k < QPT; k++) { *(T*)(tb + (x[k] ^ m0)) = b[k]; *(T*)(tb + (x[k] ^ m1)) = a[k]; }
+		for (int k = 0; k < QPT; k++)
+		{
+			*(T*)(tb + (x[k] ^ m0)) = SG ? P::negif(b[k], sg[k]) : b[k];
+			*(T*)(tb + (x[k] ^ m1)) = SG ? P::negif(a[k], sg[k]) : a[k];
+		}
 		return;
 	case BK_NEG1:
 #pragma unroll
@@ -618,7 +642,11 @@ __device__ __forceinline__ void tgt_block(char* tb, const unsigned (&x)[QPT], un
 #pragma unroll
 		for (int k = 0; k < QPT; k++) { a[k] = *(T*)(tb + (x[k] ^ m0)); b[k] = *(T*)(tb + (x[k] ^ m1)); }
 #pragma unroll
-		for (int k = 0; k < QPT; k++) { *(T*)(tb + (x[k] ^ m0)) = P::mul(c1, b[k]); *(T*)(tb + (x[k] ^ m1)) = P::mul(c2, a[k]); }
+		for (int k = 0; k < QPT; k++)
+		{
+			if (SG) { a[k] = P::negif(a[k], sg[k]); b[k] = P::negif(b[k], sg[k]); }
+			*(T*)(tb + (x[k] ^ m0)) = P::mul(c1, b[k]); *(T*)(tb + (x[k] ^ m1)) = P::mul(c2, a[k]);
+		}
 		return;
 	}
 	case BK_RI:
@@ -631,8 +659,9 @@ __device__ __forceinline__ void tgt_block(char* tb, const unsigned (&x)[QPT], un
 #pragma unroll
 			for (int k = 0; k < QPT; k++)
 			{
-				*(T*)(tb + (x[k] ^ m0)) = P::madd2_ri(c0, false, a[k], c1, true, b[k]);
-				*(T*)(tb + (x[k] ^ m1)) = P::madd2_ri(c2, true, a[k], c3, false, b[k]);
+				const T bs = SG ? P::negif(b[k], sg[k]) : b[k], as = SG ? P::negif(a[k], sg[k]) : a[k];
+				*(T*)(tb + (x[k] ^ m0)) = P::madd2_ri(c0, false, a[k], c1, true, bs);
+				*(T*)(tb + (x[k] ^ m1)) = P::madd2_ri(c2, true, as, c3, false, b[k]);
 			}
 		}
 		else
@@ -640,8 +669,9 @@ __device__ __forceinline__ void tgt_block(char* tb, const unsigned (&x)[QPT], un
 #pragma unroll
 			for (int k = 0; k < QPT; k++)
 			{
-				*(T*)(tb + (x[k] ^ m0)) = P::madd2_ri(c0, rot & 1, a[k], c1, rot & 2, b[k]);
-				*(T*)(tb + (x[k] ^ m1)) = P::madd2_ri(c2, rot & 4, a[k], c3, rot & 8, b[k]);
+				const T bs = SG ? P::negif(b[k], sg[k]) : b[k], as = SG ? P::negif(a[k], sg[k]) : a[k];
+				*(T*)(tb + (x[k] ^ m0)) = P::madd2_ri(c0, rot & 1, a[k], c1, rot & 2, bs);
+				*(T*)(tb + (x[k] ^ m1)) = P::madd2_ri(c2, rot & 4, as, c3, rot & 8, b[k]);
 			}
 		}
 		return;
@@ -654,17 +684,18 @@ __device__ __forceinline__ void tgt_block(char* tb, const unsigned (&x)[QPT], un
 #pragma unroll
 		for (int k = 0; k < QPT; k++)
 		{
-			*(T*)(tb + (x[k] ^ m0)) = P::madd2(c0, a[k], c1, b[k]);
-			*(T*)(tb + (x[k] ^ m1)) = P::madd2(c2, a[k], c3, b[k]);
+			const T bs = SG ? P::negif(b[k], sg[k]) : b[k], as = SG ? P::negif(a[k], sg[k]) : a[k];
+			*(T*)(tb + (x[k] ^ m0)) = P::madd2(c0, a[k], c1, bs);
+			*(T*)(tb + (x[k] ^ m1)) = P::madd2(c2, as, c3, b[k]);
 		}
 	}
 	}
 }
 
 // one target gate on the tile: QPT quartets per thread, q = t + k * blockDim.x
-// (QPT * blockDim.x == number of quartets)
+// (QPT * blockDim.x == number of quartets); nlb: the tile's nonlocal compact bits
 template <class P, int QPT>
-__device__ __forceinline__ void tgt_gate(char* tb, const TGate& r, const typename P::T* mats, int tpar)
+__device__ __forceinline__ void tgt_gate(char* tb, const TGate& r, const typename P::T* mats, int tpar, unsigned nlb)
 {
 	constexpr int ES = sizeof(typename P::T);
 	const unsigned MW = r.m.x, MY = r.m.y, MZ = r.m.z, SCX = r.m.w;
@@ -684,47 +715,73 @@ __device__ __forceinline__ void tgt_gate(char* tb, const TGate& r, const typenam
 	}
 	const int kw = r.h.x >> 13;
 	const typename P::T* m = mats + (size_t)r.h.y * 8;
-	tgt_block<P, QPT>(tb, x, 0u, MW, (kw >> 3) & 7, (kw >> 10) & 15, m + 4);
-	tgt_block<P, QPT>(tb, x, MY, MZ, kw & 7, (kw >> 6) & 15, m);
+	unsigned sg[QPT];
+	if (r.sl | r.snl)
+	{
+		// parity of the string bits of each quartet's corner pair; the string bits are
+		// not among the quartet's two bits, except that a string through the dropped
+		// qubit (gates on two compact wires only) differs by one between the corner and
+		// the center pair
+		const unsigned ml = (unsigned)r.sl & 0xffffu, md = ((unsigned)r.sl >> 16) & 1u, sp = ((unsigned)r.sl >> 17) & 7u;
+		const unsigned s0 = (unsigned)(__popc(b0 & ml) + __popc(nlb & (unsigned)r.snl)) ^ (md ? p0 : 0u);
+#pragma unroll
+		for (int k = 0; k < QPT; k++)
+			sg[k] = (s0 ^ ((k & 1) ? sp : 0u) ^ ((k & 2) ? (sp >> 1) : 0u) ^ ((k & 4) ? (sp >> 2) : 0u)) & 1u;
+		tgt_block<P, QPT, true>(tb, x, 0u, MW, (kw >> 3) & 7, (kw >> 10) & 15, m + 4, sg);
+#pragma unroll
+		for (int k = 0; k < QPT; k++) sg[k] ^= md;
+		tgt_block<P, QPT, true>(tb, x, MY, MZ, kw & 7, (kw >> 6) & 15, m, sg);
+	}
+	else
+	{
+		tgt_block<P, QPT, false>(tb, x, 0u, MW, (kw >> 3) & 7, (kw >> 10) & 15, m + 4, sg);
+		tgt_block<P, QPT, false>(tb, x, MY, MZ, kw & 7, (kw >> 6) & 15, m, sg);
+	}
 }
 
 // the same with one quartet per iteration, for tiles whose quartet count is not 4 or 8
 // times the block size
 template <class P>
-__device__ __forceinline__ void tgt_gate_any(char* tb, const TGate& r, const typename P::T* mats, int tpar, unsigned Q)
+__device__ __forceinline__ void tgt_gate_any(char* tb, const TGate& r, const typename P::T* mats, int tpar, unsigned nlb, unsigned Q)
 {
 	constexpr int ES = sizeof(typename P::T);
 	const unsigned MW = r.m.x, MY = r.m.y, MZ = r.m.z, SCX = r.m.w;
 	const int lo = r.h.x & 31, hi = (r.h.x >> 5) & 31;
 	const int kw = r.h.x >> 13;
 	const typename P::T* m = mats + (size_t)r.h.y * 8;
+	const unsigned ml = (unsigned)r.sl & 0xffffu, md = ((unsigned)r.sl >> 16) & 1u;
+	const unsigned sn = (unsigned)__popc(nlb & (unsigned)r.snl);
 	for (unsigned q = threadIdx.x; q < Q; q += blockDim.x)
 	{
 		const unsigned e = ins0u(ins0u(q, lo), hi);
-		const unsigned x[1] = { (tsw<ES>(e) * ES) ^ (((__popc(e) + tpar) & 1) ? SCX : 0u) };
-		tgt_block<P, 1>(tb, x, 0u, MW, (kw >> 3) & 7, (kw >> 10) & 15, m + 4);
-		tgt_block<P, 1>(tb, x, MY, MZ, kw & 7, (kw >> 6) & 15, m);
+		const unsigned pe = (unsigned)(__popc(e) + tpar) & 1u;
+		const unsigned x[1] = { (tsw<ES>(e) * ES) ^ (pe ? SCX : 0u) };
+		const unsigned sgk[1] = { ((unsigned)__popc(e & ml) + sn + (md ? pe : 0u)) & 1u };
+		const unsigned sgc[1] = { sgk[0] ^ md };
+		tgt_block<P, 1, true>(tb, x, 0u, MW, (kw >> 3) & 7, (kw >> 10) & 15, m + 4, sgk);
+		tgt_block<P, 1, true>(tb, x, MY, MZ, kw & 7, (kw >> 6) & 15, m, sgc);
 	}
 }
 
 // the gates [gbeg, gend) of a pass on one tile, records read one gate ahead
 template <class P, int QPT>
-__device__ __forceinline__ void tgt_gates(char* tb, const TGate* gates, int gbeg, int gend, const typename P::T* mats, int tpar, unsigned Q)
+__device__ __forceinline__ void tgt_gates(char* tb, const TGate* gates, int gbeg, int gend, const typename P::T* mats, int tpar,
+	unsigned nlb, unsigned Q)
 {
 	if (gbeg >= gend) return;
 	TGate r = gates[gbeg];
 	for (int gi = gbeg; gi < gend; gi++)
 	{
 		const TGate rn = gates[min(gi + 1, gend - 1)];
-		if (QPT > 0) tgt_gate<P, (QPT > 0 ? QPT : 1)>(tb, r, mats, tpar);
-		else tgt_gate_any<P>(tb, r, mats, tpar, Q);
+		if (QPT > 0) tgt_gate<P, (QPT > 0 ? QPT : 1)>(tb, r, mats, tpar, nlb);
+		else tgt_gate_any<P>(tb, r, mats, tpar, nlb, Q);
 		__syncthreads();
 		r = rn;
 	}
 }
 
-template <class P>
-__global__ void __launch_bounds__(256, 2) k_target(Args<P> a)
+template <class P, int NT>
+__global__ void __launch_bounds__(NT, 512 / NT) k_target(Args<P> a)
 {
 	typedef typename P::T T;
 	constexpr int ES = sizeof(T);
@@ -778,9 +835,9 @@ __global__ void __launch_bounds__(256, 2) k_target(Args<P> a)
 						}
 					}
 				__syncthreads();
-				if (qpt == 4) tgt_gates<P, 4>(tb, a.utg, pr.gbeg, pr.gend, pm, tpar, Q);
-				else if (qpt == 8) tgt_gates<P, 8>(tb, a.utg, pr.gbeg, pr.gend, pm, tpar, Q);
-				else tgt_gates<P, 0>(tb, a.utg, pr.gbeg, pr.gend, pm, tpar, Q);
+				if (qpt == 4) tgt_gates<P, 4>(tb, a.utg, pr.gbeg, pr.gend, pm, tpar, nlb, Q);
+				else if (qpt == 8) tgt_gates<P, 8>(tb, a.utg, pr.gbeg, pr.gend, pm, tpar, nlb, Q);
+				else tgt_gates<P, 0>(tb, a.utg, pr.gbeg, pr.gend, pm, tpar, nlb, Q);
 				for (unsigned e = threadIdx.x; e < n; e += blockDim.x)
 				{
 					const T v = tile[tsw<ES>(e)];
@@ -1174,7 +1231,91 @@ struct mgcu_target
 	DevBuf res_cols[3];            // resident -conj(U e_b) per precision
 	int res_kt[3] = { -1, -1, -1 };
 	bool res_valid[3] = { false, false, false };
+	// the gate list the target sweep runs (fermionic swaps relabelled away, see
+	// relabel_fswaps) with per-gate Jordan-Wigner string wires
+	bool sweep_ready = false;
+	std::vector<mgg> sg;
+	std::vector<int> sw;
+	std::vector<unsigned> smask;
 };
+
+// Remove fermionic swaps (center [[0,1],[1,0]], corner diag(1,-1)) from a circuit
+// exactly.  An fswap on wires (X, Y) is a SWAP, absorbed by relabelling the logical
+// wires of all later gates, times CZ(X, Y).  Each pending CZ is moved past the later
+// gates: a gate on both of its wires absorbs it (corner block times diag(1,-1) on the
+// right); a gate on one of them, (X, u) with the CZ on (X, v), becomes the gate with
+// its off-diagonal entries negated when wire v is 1 (v joins the gate's string);
+// other gates commute with it.  Applies only when the relabelling ends at the identity
+// (true for fswap networks that restore the qubit order, such as Jordan-Wigner hops);
+// CZs still pending at the end are appended as gates.  Returns false (and leaves the
+// outputs empty) when the circuit has no fswap or the order is not restored.
+static bool relabel_fswaps(int L, const std::vector<mgg>& gates, const std::vector<int>& wires,
+	std::vector<mgg>& og, std::vector<int>& ow, std::vector<unsigned>& om)
+{
+	auto is = [](mgc z, double re, double im) { return z.re == re && z.im == im; };
+	auto fswap = [&](const mgg& g) {
+		return is(g.c[0], 0, 0) && is(g.c[1], 1, 0) && is(g.c[2], 1, 0) && is(g.c[3], 0, 0)
+			&& is(g.k[0], 1, 0) && is(g.k[1], 0, 0) && is(g.k[2], 0, 0) && is(g.k[3], -1, 0);
+	};
+	og.clear(); ow.clear(); om.clear();
+	bool any = false;
+	for (const mgg& g : gates) any = any || fswap(g);
+	if (!any || L > 32) return false;
+	std::vector<int> pi(L);
+	for (int q = 0; q < L; q++) pi[q] = q;
+	std::vector<std::pair<int, int>> cz;   // pending CZs on physical wires (u < v)
+	for (size_t i = 0; i < gates.size(); i++)
+	{
+		const int X = pi[wires[2 * i]], Y = pi[wires[2 * i + 1]];
+		if (fswap(gates[i]))
+		{
+			const std::pair<int, int> c(std::min(X, Y), std::max(X, Y));
+			auto it = std::find(cz.begin(), cz.end(), c);
+			if (it != cz.end()) cz.erase(it); else cz.push_back(c);
+			std::swap(pi[wires[2 * i]], pi[wires[2 * i + 1]]);
+			continue;
+		}
+		mgg g = gates[i];
+		unsigned mask = 0;
+		for (size_t j = 0; j < cz.size();)
+		{
+			const int u = cz[j].first, v = cz[j].second;
+			const bool hu = (u == X || u == Y), hv = (v == X || v == Y);
+			if (hu && hv)
+			{
+				g.k[1] = mgc_make(-g.k[1].re, -g.k[1].im);
+				g.k[3] = mgc_make(-g.k[3].re, -g.k[3].im);
+				cz.erase(cz.begin() + j);
+				continue;
+			}
+			if (hu) mask ^= 1u << v;
+			else if (hv) mask ^= 1u << u;
+			j++;
+		}
+		og.push_back(g); ow.push_back(X); ow.push_back(Y); om.push_back(mask);
+	}
+	for (int q = 0; q < L; q++)
+		if (pi[q] != q) { og.clear(); ow.clear(); om.clear(); return false; }
+	for (const auto& c : cz)
+	{
+		mgg g;
+		for (int q = 0; q < 4; q++) { g.c[q] = mgc_make(q == 0 || q == 3 ? 1 : 0, 0); g.k[q] = mgc_make(0, 0); }
+		g.k[0] = mgc_make(1, 0); g.k[3] = mgc_make(-1, 0);
+		og.push_back(g); ow.push_back(c.first); ow.push_back(c.second); om.push_back(0);
+	}
+	return true;
+}
+
+static void prepare_sweep(mgcu_target* t)
+{
+	if (t->sweep_ready) return;
+	if (!relabel_fswaps(t->L, t->gates, t->wires, t->sg, t->sw, t->smask))
+	{
+		t->sg = t->gates; t->sw = t->wires;
+		t->smask.assign(t->gates.size(), 0u);
+	}
+	t->sweep_ready = true;
+}
 
 template <class P>
 static int upload_mats(const mgg* gates, int ng, DevBuf& buf)
@@ -1214,16 +1355,18 @@ static int target_prog(mgcu_target* t, int kt, int threads, TargetProg*& out)
 	if (tp.kt != kt || tp.threads != threads)
 	{
 		typedef typename P::T T;
-		schedule(t->L, kt, t->wires.data(), (int)t->gates.size(), true, tp.sched, sizeof(T) >= 16 ? 1 : 2);
+		prepare_sweep(t);
+		const std::vector<mgg>& gates = t->sg;
+		schedule(t->L, kt, t->sw.data(), (int)gates.size(), true, tp.sched, sizeof(T) >= 16 ? 1 : 2, t->smask.data());
 		// distinct matrices, then passes split so that each stages at most MAXPM of them
-		const int ngt = (int)t->gates.size();
+		const int ngt = (int)gates.size();
 		std::vector<int> uid(std::max(ngt, 1), 0);
 		{
 			std::map<std::array<double, 16>, int> seen;
 			for (int g = 0; g < ngt; g++)
 			{
 				std::array<double, 16> key;
-				memcpy(key.data(), &t->gates[g], sizeof(key));
+				memcpy(key.data(), &gates[g], sizeof(key));
 				auto it = seen.emplace(key, (int)seen.size()).first;
 				uid[g] = it->second;
 			}
@@ -1268,7 +1411,7 @@ static int target_prog(mgcu_target* t, int kt, int threads, TargetProg*& out)
 		int e = upload_sched(tp.sched, tp.pass, tp.gate);
 		if (e) return e;
 		std::vector<int> kw;
-		e = upload_target_mats<P>(t->gates.data(), (int)t->gates.size(), tp.mats, tp.kinds, kw);
+		e = upload_target_mats<P>(gates.data(), ngt, tp.mats, tp.kinds, kw);
 		if (e) return e;
 		// k_target's records; the auxiliary bit of a gate on the dropped qubit is a high
 		// tile bit, away from the swizzle's two conflicting low pairs
@@ -1276,15 +1419,35 @@ static int target_prog(mgcu_target* t, int kt, int threads, TargetProg*& out)
 		auto ins0 = [](unsigned v, int pos) { return ((v >> pos) << (pos + 1)) | (v & ((1u << pos) - 1u)); };
 		std::vector<TGate> tg(std::max<size_t>(tp.sched.gate.size(), 1));
 		memset(tg.data(), 0, sizeof(TGate) * tg.size());
+		std::vector<int> pass_of_rec(tp.sched.gate.size(), 0);
+		for (size_t p = 0; p < tp.sched.pass.size(); p++)
+			for (int i = tp.sched.pass[p].gbeg; i < tp.sched.pass[p].gend; i++) pass_of_rec[i] = (int)p;
 		for (size_t i = 0; i < tp.sched.gate.size(); i++)
 		{
 			const GateRec& r = tp.sched.gate[i];
+			const PassRec& pr = tp.sched.pass[pass_of_rec[i]];
+			// the gate's string split into local positions, nonlocal compact bits and the
+			// dropped qubit
+			unsigned ml = 0, mnl = 0, md = 0;
+			for (int q = 0; q < t->L; q++)
+			{
+				if (!(t->smask[r.g] & (1u << q))) continue;
+				if (q == t->L - 1) { md = 1; continue; }
+				const int cbit = t->L - 2 - q;
+				int lp = -1;
+				for (int j = 0; j < kt; j++) if (pr.lbits[j] == cbit) lp = j;
+				if (lp >= 0) ml |= 1u << lp; else mnl |= 1u << cbit;
+			}
 			int pa, pb;
 			if (r.type == 0) { pa = r.la; pb = r.lb; }
 			else
 			{
+				// auxiliary bit: a high tile bit outside the gate's string
 				pa = r.type == 1 ? r.la : r.lb;
-				pb = (pa == kt - 1) ? kt - 2 : kt - 1;
+				pb = -1;
+				for (int j = kt - 1; j >= 0 && pb < 0; j--)
+					if (j != pa && !(ml & (1u << j))) pb = j;
+				if (pb < 0) { mg_set_error("no auxiliary tile bit outside a gate's string"); return MG_ERR_ARG; }
 			}
 			const int lo = std::min(pa, pb), hi = std::max(pa, pb);
 			const unsigned SA = tsw<ES>(1u << pa) * ES, SB = tsw<ES>(1u << pb) * ES;
@@ -1293,16 +1456,20 @@ static int target_prog(mgcu_target* t, int kt, int threads, TargetProg*& out)
 			o.m.y = (int)(r.type == 2 ? (SA ^ SB) : SB);
 			o.m.z = (int)(r.type == 0 ? SA : (r.type == 1 ? (SA ^ SB) : SB));
 			o.m.w = (int)(r.type == 0 ? 0u : SB);
-			unsigned d[3], dpar = 0;
+			unsigned d[3], dpar = 0, spar = 0;
 			for (int k = 0; k < 3; k++)
 			{
 				const unsigned e = ins0(ins0((unsigned)threads << k, lo), hi);
 				d[k] = tsw<ES>(e) * ES;
-				dpar |= (unsigned)(__builtin_popcount(e) & 1) << k;
+				const unsigned pe = (unsigned)(__builtin_popcount(e) & 1);
+				dpar |= pe << k;
+				spar |= ((unsigned)(__builtin_popcount(e & ml) & 1) ^ (md & pe)) << k;
 			}
 			o.h.x = lo | hi << 5 | (int)(dpar << 10) | kw[r.g] << 13;
 			o.h.y = slot[i];
 			o.h.z = (int)d[0]; o.h.w = (int)d[1]; o.d4 = (int)d[2];
+			o.sl = (int)(ml | md << 16 | spar << 17);
+			o.snl = (int)mnl;
 		}
 		e = tp.tg.alloc(sizeof(TGate) * tg.size());
 		if (e) return e;
@@ -1313,8 +1480,8 @@ static int target_prog(mgcu_target* t, int kt, int threads, TargetProg*& out)
 		{
 			mgc sc[4], sk[4];
 			unsigned rc, rk;
-			classify_block(t->gates[pm_first[i]].c, rc, sc);
-			classify_block(t->gates[pm_first[i]].k, rk, sk);
+			classify_block(gates[pm_first[i]].c, rc, sc);
+			classify_block(gates[pm_first[i]].k, rk, sk);
 			for (int q = 0; q < 4; q++)
 			{
 				hm[i * 8 + q] = P::make(sc[q].re, sc[q].im);
@@ -1385,7 +1552,12 @@ struct mgcu_plan
 	std::vector<int> wires, block, place;
 	std::vector<double> place_w;
 	int L, nb, kt, threads, grid_a, grid_b, grid_t, prec;
-	size_t smem_t;                 // k_target: smem plus MAXPM staged matrices
+	int kt_t, threads_t;           // k_target's tile bits and block size
+	size_t smem_t;                 // k_target: its tile, tables, scratch and MAXPM staged matrices
+	bool ktime = false;            // record events around k_target launches (mgcu_plan_time_ms)
+	std::vector<cudaEvent_t> kev;  // start/stop pairs
+	size_t kev_used = 0;
+	~mgcu_plan() { for (cudaEvent_t ev : kev) cudaEventDestroy(ev); }
 	long S;
 	size_t tsize;
 	size_t smem;
@@ -1407,21 +1579,31 @@ static int launch_target(mgcu_plan* p, long b0, long b1, typename P::T* out)
 	MgcuContext* c = mgcu_ctx();
 	Args<P> a;
 	memset(&a, 0, sizeof(a));
-	a.L = p->L; a.nb = p->nb; a.kt = p->kt; a.S = p->S;
+	a.L = p->L; a.nb = p->nb; a.kt = p->kt_t; a.S = p->S;
 	TargetProg* tp = nullptr;
-	int e = target_prog<P>(p->d.target, p->kt, p->threads, tp);
+	int e = target_prog<P>(p->d.target, p->kt_t, p->threads_t, tp);
 	if (e) return e;
 	a.U.pass = tp->pass.as<PassRec>(); a.U.gate = tp->gate.as<GateRec>(); a.U.npass = (int)tp->sched.pass.size();
 	a.um = tp->mats.as<T>();
 	a.utg = tp->tg.as<TGate>();
 	a.upm = tp->pm.as<int2>();
 	a.upmats = tp->pmats.as<T>();
-	a.pm_off = (unsigned)p->smem;
+	a.pm_off = (unsigned)(p->smem_t - (size_t)MAXPM * 8 * p->tsize);
 	a.b0 = b0; a.b1 = b1;
 	a.ucols = out;
 	const int grid = (int)std::min<long>(p->grid_t, b1 - b0);
-	k_target<P><<<grid, p->threads, p->smem_t, c->stream>>>(a);
+	if (p->ktime)
+		while (p->kev.size() < p->kev_used + 2)
+		{
+			cudaEvent_t ev;
+			MGCU_TRY(cudaEventCreate(&ev));
+			p->kev.push_back(ev);
+		}
+	if (p->ktime) MGCU_TRY(cudaEventRecord(p->kev[p->kev_used], c->stream));
+	if (p->threads_t > 256) k_target<P, 512><<<grid, p->threads_t, p->smem_t, c->stream>>>(a);
+	else k_target<P, 256><<<grid, p->threads_t, p->smem_t, c->stream>>>(a);
 	MGCU_LAUNCHED();
+	if (p->ktime) { MGCU_TRY(cudaEventRecord(p->kev[p->kev_used + 1], c->stream)); p->kev_used += 2; }
 	return 0;
 }
 
@@ -1469,18 +1651,20 @@ static int set_smem_attr()
 {
 	MgcuContext* c = mgcu_ctx();
 	MGCU_TRY(cudaFuncSetAttribute(k_columns<P, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)std::min<size_t>(c->smem_optin, 227 * 1024)));
-	MGCU_TRY(cudaFuncSetAttribute(k_target<P>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)std::min<size_t>(c->smem_optin, 227 * 1024)));
+	MGCU_TRY(cudaFuncSetAttribute(k_target<P, 256>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)std::min<size_t>(c->smem_optin, 227 * 1024)));
+	MGCU_TRY(cudaFuncSetAttribute(k_target<P, 512>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)std::min<size_t>(c->smem_optin, 227 * 1024)));
 	MGCU_TRY(cudaFuncSetAttribute(k_hessian<P>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)std::min<size_t>(c->smem_optin, 227 * 1024)));
 	return 0;
 }
 
 template <class P>
-static int occupancy(int threads, size_t smem, size_t smem_t, int& per_sm, int& per_sm_target)
+static int occupancy(int threads, size_t smem, int threads_t, size_t smem_t, int& per_sm, int& per_sm_target)
 {
 	int n1 = 0, n2 = 0, n3 = 0;
 	MGCU_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n1, k_columns<P, false>, threads, smem));
 	MGCU_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n2, k_hessian<P>, threads, smem));
-	MGCU_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n3, k_target<P>, threads, smem_t));
+	if (threads_t > 256) MGCU_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n3, k_target<P, 512>, threads_t, smem_t));
+	else MGCU_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n3, k_target<P, 256>, threads_t, smem_t));
 	per_sm = std::max(1, std::min(n1, n2));
 	per_sm_target = std::max(1, n3);
 	return 0;
@@ -1529,16 +1713,29 @@ extern "C" mgcu_plan* mgcu_plan_create(const mgcu_plan_desc* d)
 	const long opt_thr = mgcu_option(MG_OPT_THREADS_ID);
 	if (opt_thr > 0) threads = (int)std::max(32L, std::min(256L, (opt_thr / 32) * 32));
 	p->threads = threads;
-	// tile, deposit tables, reduction scratch (also k_target's 16 staged gate entries)
-	p->smem = ((size_t)1 << p->kt) * p->tsize + 2 * 128 * sizeof(unsigned) + std::max<size_t>((size_t)(threads / 32) * 16 * sizeof(double), 16 * 16);
+	// tile, deposit tables, reduction scratch
+	p->smem = ((size_t)1 << p->kt) * p->tsize + 2 * 128 * sizeof(unsigned) + (size_t)(threads / 32) * 16 * sizeof(double);
 
 	schedule(p->L, p->kt, p->wires.data(), d->ngates, false, p->ws);
 
-	p->smem_t = p->smem + (size_t)MAXPM * 8 * p->tsize;
+	// the target sweep's own tile and block size (circuit targets only)
+	{
+		int ktt = p->kt;
+		const long o = mgcu_option(MG_OPT_TARGET_TILE_BITS_ID);
+		if (o > 0) ktt = (int)std::max(5L, std::min<long>(o, MAXKT));
+		while (ktt > 5 && ((size_t)1 << ktt) * p->tsize > 128 * 1024) ktt--;
+		p->kt_t = std::min(ktt, p->nb);
+		int tt = std::max(32, std::min(256, 1 << (p->kt_t - 2)));
+		const long ot = mgcu_option(MG_OPT_TARGET_THREADS_ID);
+		if (ot > 0) tt = (int)std::max(32L, std::min(512L, (ot / 32) * 32));
+		p->threads_t = tt;
+		p->smem_t = ((size_t)1 << p->kt_t) * p->tsize + 2 * 128 * sizeof(unsigned)
+			+ std::max<size_t>((size_t)(tt / 32) * 16 * sizeof(double), 16 * 16) + (size_t)MAXPM * 8 * p->tsize;
+	}
 	int per_sm = 1, per_sm_t = 1, e = 0;
-	if (p->prec == MG_PREC_FP64_ID) { e = set_smem_attr<PrecD>(); if (!e) e = occupancy<PrecD>(threads, p->smem, p->smem_t, per_sm, per_sm_t); }
-	else if (p->prec == MG_PREC_FP32_ID) { e = set_smem_attr<PrecF>(); if (!e) e = occupancy<PrecF>(threads, p->smem, p->smem_t, per_sm, per_sm_t); }
-	else { e = set_smem_attr<PrecX>(); if (!e) e = occupancy<PrecX>(threads, p->smem, p->smem_t, per_sm, per_sm_t); }
+	if (p->prec == MG_PREC_FP64_ID) { e = set_smem_attr<PrecD>(); if (!e) e = occupancy<PrecD>(threads, p->smem, p->threads_t, p->smem_t, per_sm, per_sm_t); }
+	else if (p->prec == MG_PREC_FP32_ID) { e = set_smem_attr<PrecF>(); if (!e) e = occupancy<PrecF>(threads, p->smem, p->threads_t, p->smem_t, per_sm, per_sm_t); }
+	else { e = set_smem_attr<PrecX>(); if (!e) e = occupancy<PrecX>(threads, p->smem, p->threads_t, p->smem_t, per_sm, per_sm_t); }
 	if (e) { delete p; return nullptr; }
 	const long opt_cps = mgcu_option(MG_OPT_CTAS_PER_SM_ID);
 	if (opt_cps > 0) per_sm = (int)std::min<long>(per_sm, opt_cps);
@@ -1734,6 +1931,9 @@ extern "C" double mgcu_plan_time_ms(mgcu_plan* p, long b0, long b1, int steps, i
 {
 	MgcuContext* c = mgcu_ctx();
 	if (flush_l2 && p->flush.alloc(512ull << 20)) return -1;
+	p->ktime = true;
+	p->kev_used = 0;
+	struct Off { mgcu_plan* p; ~Off() { p->ktime = false; } } off{ p };
 	double total = 0;
 	for (int s = 0; s < steps; s++)
 	{
@@ -1747,6 +1947,21 @@ extern "C" double mgcu_plan_time_ms(mgcu_plan* p, long b0, long b1, int steps, i
 		total += ms;
 	}
 	return total;
+}
+
+// k_target launches of the last mgcu_plan_time_ms: their number and summed duration
+extern "C" int mgcu_plan_target_kernel_ms(mgcu_plan* p, double* ms, long* launches)
+{
+	double t = 0;
+	for (size_t i = 0; i + 1 < p->kev_used; i += 2)
+	{
+		float m = 0;
+		MGCU_TRY(cudaEventElapsedTime(&m, p->kev[i], p->kev[i + 1]));
+		t += m;
+	}
+	*ms = t;
+	*launches = (long)(p->kev_used / 2);
+	return 0;
 }
 
 // ======================================================================================

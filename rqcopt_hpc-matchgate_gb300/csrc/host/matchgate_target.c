@@ -127,7 +127,7 @@ typedef struct
 {
 	uint64_t hash;
 	int L, ngates, nblocks, want_grad, want_hess, ti, precision;
-	long opts[5];
+	long opts[MG_NOPTIONS + 1];
 	mgcu_target* target;
 	int* wires;
 	int* block;
@@ -192,8 +192,8 @@ static mgcu_plan* get_plan(int L, int ngates, const int* wires, int nblocks, con
 	mgcu_target* target)
 {
 	const int prec = mgcu_precision();
-	long opts[5];
-	for (int o = 1; o <= 4; o++) opts[o] = mgcu_option(o);
+	long opts[MG_NOPTIONS + 1];
+	for (int o = 1; o <= MG_NOPTIONS; o++) opts[o] = mgcu_option(o);
 	opts[0] = 0;
 	uint64_t h = 1469598103934665603ull;
 	h = fnv(h, wires, sizeof(int) * 2 * ngates);
@@ -608,4 +608,13 @@ double mg_plan_time_ms(mg_plan* pl, int steps, int flush_l2)
 	double r = mgcu_plan_time_ms(pl->p, 0, 1L << pl->L, steps, flush_l2);
 	mgcu_unlock();
 	return r;
+}
+
+int mg_plan_target_kernel_ms(mg_plan* pl, double* ms, long* launches)
+{
+	if (!pl || !ms || !launches) { mg_set_error("mg_plan_target_kernel_ms: null argument"); return MG_ERR_ARG; }
+	mgcu_lock();
+	const int e = mgcu_plan_target_kernel_ms(pl->p, ms, launches);
+	mgcu_unlock();
+	return e ? MG_ERR_DEVICE : 0;
 }

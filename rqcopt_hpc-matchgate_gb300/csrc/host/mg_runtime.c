@@ -50,7 +50,7 @@ int mgcu_precision(void) { return g_precision; }
 
 int mg_set_option(int option, long value)
 {
-	if (option < 1 || option > 4 || value < 0)
+	if (option < 1 || option > MG_NOPTIONS || value < 0)
 	{
 		mg_set_error("invalid option %d = %ld", option, value);
 		return MG_ERR_ARG;
@@ -61,7 +61,7 @@ int mg_set_option(int option, long value)
 	return 0;
 }
 
-long mg_get_option(int option) { return (option >= 1 && option <= 4) ? g_options[option] : -1; }
+long mg_get_option(int option) { return (option >= 1 && option <= MG_NOPTIONS) ? g_options[option] : -1; }
 long mgcu_option(int option) { return mg_get_option(option); }
 
 long mg_launch_count(void) { return mgcu_launch_count(); }

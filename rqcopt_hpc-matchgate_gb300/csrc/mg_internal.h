@@ -30,6 +30,9 @@ extern "C" {
 #define MG_OPT_THREADS_ID       2
 #define MG_OPT_CHUNK_COLUMNS_ID 3
 #define MG_OPT_CTAS_PER_SM_ID   4
+#define MG_OPT_TARGET_TILE_BITS_ID 5
+#define MG_OPT_TARGET_THREADS_ID   6
+#define MG_NOPTIONS             6
 
 /* ---- runtime ---- */
 void mg_set_error(const char* fmt, ...);
@@ -97,6 +100,7 @@ int mgcu_plan_fetch(mgcu_plan* p, mgc* f, mgg* dblocks, mgc* hess);
 int mgcu_plan_project(mgcu_plan* p, const mgg* vblocks, double* grad_vec, double* H);
 long mgcu_plan_chunk_columns(const mgcu_plan* p);
 double mgcu_plan_time_ms(mgcu_plan* p, long b0, long b1, int steps, int flush_l2);
+int mgcu_plan_target_kernel_ms(mgcu_plan* p, double* ms, long* launches);
 
 /* ---- FP64 algebra on the GPU ---- */
 int mgcu_retract(const mgg* u, const double* eta, int n, mgg* v);

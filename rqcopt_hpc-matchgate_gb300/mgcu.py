@@ -22,6 +22,7 @@ DEFAULT_LIB = os.path.join(HERE, "_build", "libmgcu.so")
 
 PREC_FP64, PREC_MIXED, PREC_FP32 = 0, 1, 2
 OPT_TILE_BITS, OPT_THREADS, OPT_CHUNK_COLUMNS, OPT_CTAS_PER_SM = 1, 2, 3, 4
+OPT_TARGET_TILE_BITS, OPT_TARGET_THREADS = 5, 6
 EVAL_TARGET, EVAL_GRADIENT, EVAL_HESSIAN, EVAL_TI = 0, 1, 2, 4
 
 P = C.c_void_p
@@ -115,6 +116,7 @@ class MatchgateLib:
             L.mg_plan_free.argtypes = [P]
             L.mg_plan_time_ms.argtypes = [P, C.c_int, C.c_int]
             L.mg_plan_time_ms.restype = C.c_double
+            L.mg_plan_target_kernel_ms.argtypes = [P, P, P]
             L.mg_launch_count.restype = C.c_long
             L.mg_get_option.restype = C.c_long
             L.mg_set_option.argtypes = [C.c_int, C.c_long]
@@ -137,6 +139,14 @@ class MatchgateLib:
 
     def last_error(self):
         return self.lib.mg_last_error().decode()
+
+    def plan_target_kernel_ms(self, plan):
+        """(summed ms, launches) of the target-sweep kernel in the last plan timing"""
+        ms, n = C.c_double(), C.c_long()
+        rc = self.lib.mg_plan_target_kernel_ms(P(plan), C.byref(ms), C.byref(n))
+        if rc != 0:
+            raise RuntimeError(self.last_error())
+        return ms.value, n.value
 
     def launch_count(self):
         return self.lib.mg_launch_count()

@@ -417,7 +417,8 @@ def test_hubbard_target_vs_oracle(lib, oracle):
 @pytest.mark.parametrize("L,tile_bits,threads,prec", [(10, 0, 0, mgcu.PREC_FP64), (12, 0, 0, mgcu.PREC_MIXED),
                                                       (12, 9, 0, mgcu.PREC_FP64), (14, 12, 0, mgcu.PREC_MIXED),
                                                       (14, 12, 128, mgcu.PREC_FP64), (14, 10, 0, mgcu.PREC_FP32),
-                                                      (14, 0, 0, mgcu.PREC_FP32), (14, 13, 0, mgcu.PREC_MIXED)])
+                                                      (14, 0, 0, mgcu.PREC_FP32), (14, 13, 0, mgcu.PREC_MIXED),
+                                                      (14, 13, 512, mgcu.PREC_MIXED), (14, 13, 512, mgcu.PREC_FP64)])
 def test_target_sweep_tiles_vs_oracle(lib, oracle, L, tile_bits, threads, prec):
     """the target-sweep kernel with 1, 2, 4 and 8 quartets per thread, one or several
     tiles per pass and structured and general gates (also on the dropped qubit), against
@@ -438,12 +439,62 @@ def test_target_sweep_tiles_vs_oracle(lib, oracle, L, tile_bits, threads, prec):
     t = lib.target_circuit(gates, wires, L)
     lib.set_precision(prec)
     lib.set_option(mgcu.OPT_TILE_BITS, tile_bits)
-    lib.set_option(mgcu.OPT_THREADS, threads)
+    lib.set_option(mgcu.OPT_THREADS, min(threads, 256))
+    lib.set_option(mgcu.OPT_TARGET_THREADS, threads)
     try:
         rc, f, dv = lib.brickwall_columns(lib.mg_target_apply, t, v, perms, L, *cols)
     finally:
         lib.set_option(mgcu.OPT_TILE_BITS, 0)
         lib.set_option(mgcu.OPT_THREADS, 0)
+        lib.set_option(mgcu.OPT_TARGET_THREADS, 0)
+        lib.set_precision(mgcu.PREC_FP64)
+        lib.target_free(t)
+    assert rc == 0
+    tol = 1e-4 if prec == mgcu.PREC_FP32 else 1e-12
+    f_o, dv_o = oracle.brickwall_target_and_gradient(oracle.Target("circuit", L, gates=gates, wires=wires), v, perms, L, col_range=cols)
+    sf, sg = max(1.0, abs(f_o)), max(1.0, np.max(np.abs(dv_o)))
+    assert abs(f - f_o) < tol * sf and np.max(np.abs(dv - dv_o)) < tol * sg
+
+
+def _fswap_circuit(L, n, rng, paired=True):
+    """random matchgates with fermionic swaps inserted in pairs on the same wires (the
+    qubit order is restored) or, with paired=False, one unpaired fermionic swap"""
+    fs = np.array([0, 1, 1, 0, 1, 0, 0, -1], complex)
+    gates, wires = [], []
+    while len(gates) < n:
+        a = rng.choice(L, 2, replace=False)
+        if rng.random() < 0.3:
+            gates.append(fs); wires.append(a)
+            for _ in range(3):
+                gates.append(random_gates(1, rng, unitary=True)[0]); wires.append(rng.choice(L, 2, replace=False))
+            gates.append(fs); wires.append(a[::-1] if rng.random() < 0.5 else a)
+        else:
+            gates.append(random_gates(1, rng, unitary=True)[0]); wires.append(a)
+    if not paired:
+        gates.insert(n // 2, fs); wires.insert(n // 2, np.array([0, L - 1]))
+    return np.array(gates), np.array(wires, np.int32)
+
+
+@pytest.mark.parametrize("L,prec,paired,tile_bits", [(10, mgcu.PREC_FP64, True, 0), (12, mgcu.PREC_MIXED, True, 0),
+                                                     (12, mgcu.PREC_FP64, True, 9), (12, mgcu.PREC_FP64, False, 0),
+                                                     (14, mgcu.PREC_MIXED, True, 12), (14, mgcu.PREC_FP32, True, 0)])
+def test_fswap_relabelling_vs_oracle(lib, oracle, L, prec, paired, tile_bits):
+    """targets with fermionic swaps: the sweep removes paired swaps by relabelling wires
+    and carries Jordan-Wigner strings on the gates in between (also through the dropped
+    qubit, across tiles and passes); unpaired swaps are kept as gates"""
+    rng = np.random.default_rng(200 + L + tile_bits)
+    gates, wires = _fswap_circuit(L, 120, rng, paired)
+    nl = 3
+    v = random_gates(nl, rng, unitary=True)
+    perms = brickwall_perms(L, nl, rng)
+    cols = (0, 96)
+    t = lib.target_circuit(gates, wires, L)
+    lib.set_precision(prec)
+    lib.set_option(mgcu.OPT_TILE_BITS, tile_bits)
+    try:
+        rc, f, dv = lib.brickwall_columns(lib.mg_target_apply, t, v, perms, L, *cols)
+    finally:
+        lib.set_option(mgcu.OPT_TILE_BITS, 0)
         lib.set_precision(mgcu.PREC_FP64)
         lib.target_free(t)
     assert rc == 0
