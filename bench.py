@@ -47,6 +47,10 @@ def parse():
     ap.add_argument("--fp64-columns", type=int, default=2048, help="column sample for the FP64 comparison")
     ap.add_argument("--cpu-seconds", type=float, default=15.0, help="budget of the CPU baseline sample")
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--config", default="grad16", choices=["grad16", "grad18", "hess14"],
+                    help="grad16: the headline (L=16 gradient, 5 layers); grad18: L=18 gradient, 7 layers, on a "
+                         "column sample; hess14: L=14 full Hessian, 9 layers")
+    ap.add_argument("--sample-columns", type=int, default=4096, help="column sample of --config grad18")
     ap.add_argument("--profile-columns", type=int, default=0,
                     help="small case for ncu: one evaluation over this many columns, no timing, then exit")
     return ap.parse_args()
@@ -94,7 +98,7 @@ def workload(L, nlayers, nsteps, seed=3):
 # summarised in profiles/k_target_mixed_hubbard_L16.md (608 columns, L=16, mixed); the
 # kernel's traffic is its output columns plus tile round trips that miss L2, both
 # proportional to the number of columns, so per-launch traffic = this x columns per launch
-TARGET_DRAM_BYTES_PER_COLUMN = {16: None}
+TARGET_DRAM_BYTES_PER_COLUMN = {16: (13.142094e9 + 14.298918e9) / 608}
 
 
 def alg_flops(L, gu, gw, ncols):
@@ -270,7 +274,8 @@ def run_gb300(a):
     achieved_step = flops / (ms_per_step / 1e3) / 1e12
     # dominant kernel: the target sweep (k_target), timed by CUDA events around each launch
     cols_per_launch = ncols * a.steps / tk_n
-    tk_flops = float(cols_per_launch) * (1 << (L - 1)) * 14 * gu
+    gu_run = lib.lib.mg_target_sweep_gates(mgcu.P(target))   # gates the sweep applies (fermionic swaps relabelled away)
+    tk_flops = float(cols_per_launch) * (1 << (L - 1)) * 14 * gu_run
     tk_avg_s = tk_ms / 1e3 / tk_n
     achieved = tk_flops / tk_avg_s / 1e12
     bpc = TARGET_DRAM_BYTES_PER_COLUMN.get(L) if a.precision == "mixed" else None
@@ -296,7 +301,8 @@ def run_gb300(a):
                      "kernel_ms_per_launch": tk_avg_s * 1e3, "kernel_share_of_step": tk_ms / total_ms,
                      "columns_per_launch": cols_per_launch,
                      "achieved_is": "algorithmic complex-arithmetic flops of the target sweep (14 per parity-sector "
-                                    "amplitude and gate) per second of k_target",
+                                    "amplitude and applied gate) per second of k_target",
+                     "target_gates_applied": gu_run,
                      "step_achieved": achieved_step,
                      "peak_source": "FP32 FMA microkernel of this library, measured in this run "
                                     "(MEASURED_PEAKS.json holds HBM and bf16 tensor peaks only)",
@@ -318,10 +324,65 @@ def run_gb300(a):
         print(json.dumps(out))
 
 
+def run_secondary(a):
+    """the other Hubbard configurations: L=18 gradient with 7 layers (column sample,
+    extrapolated) and L=14 gradient + full Hessian with 9 layers (504 real parameters),
+    mixed precision against FP64 on the GPU"""
+    import numpy as np
+    import mgcu
+    lib = mgcu.default_lib()
+    L, nl = (18, 7) if a.config == "grad18" else (14, 9)
+    g, w, v, perms = workload(L, nl, a.trotter_steps)
+    target = lib.target_circuit(g, w, L)
+    ncols = 1 << L
+    res = {}
+    for name, prec in (("mixed", mgcu.PREC_MIXED), ("fp64", mgcu.PREC_FP64)):
+        lib.set_precision(prec)
+        if a.config == "grad18":
+            c = min(a.sample_columns, ncols)
+            lib.brickwall_columns(lib.mg_target_apply, target, v, perms, L, 0, min(304, c))
+            t0 = time.perf_counter()
+            rc, f, dv = lib.brickwall_columns(lib.mg_target_apply, target, v, perms, L, 0, c)
+            dt = time.perf_counter() - t0
+            assert rc == 0, lib.last_error()
+            res[name] = {"evals_per_s": (c / ncols) / dt, "s_per_eval": dt * ncols / c, "f": f, "g": dv.reshape(-1)}
+        else:
+            # every gate of the brickwall its own parameter block: 8 * nl * L/2 real parameters
+            cg = np.array([v[l] for l in range(nl) for _ in range(L // 2)])
+            cw = np.array([[perms[l][2 * i], perms[l][2 * i + 1]] for l in range(nl) for i in range(L // 2)], np.int32)
+            lib.circuit_target_gradient_hessian(lib.mg_target_apply, target, cg[:1], cw[:1], L)   # warm-up
+            t0 = time.perf_counter()
+            rc, f, dg, H = lib.circuit_target_gradient_hessian(lib.mg_target_apply, target, cg, cw, L)
+            dt = time.perf_counter() - t0
+            assert rc == 0, lib.last_error()
+            res[name] = {"evals_per_s": 1 / dt, "s_per_eval": dt, "f": f, "g": dg.reshape(-1), "H": np.asarray(H)}
+    lib.target_free(target)
+    mx, fp = res["mixed"], res["fp64"]
+    rel = lambda x, y: float(np.linalg.norm(np.asarray(x) - np.asarray(y)) / np.linalg.norm(np.asarray(y)))
+    acc = {"rel_err_f_vs_fp64": abs(mx["f"] - fp["f"]) / abs(fp["f"]), "rel_err_grad_vs_fp64": rel(mx["g"], fp["g"])}
+    if "H" in mx:
+        acc["rel_err_hessian_vs_fp64"] = rel(mx["H"], fp["H"])
+    what = "gradient" if a.config == "grad18" else "gradient + per-gate Hessian"
+    out = {"metric": f"{what} evals/s at L={L} (mixed vs FP64 GPU)", "value": mx["evals_per_s"], "unit": "evals/s",
+           "n_gpus": 1, "higher_is_better": True, "dtype": "f32 float-float pairs, f64 final sums",
+           "data": "synthetic (seeded Hubbard Trotter target, seeded near-identity fit)",
+           "config": {"workload": f"L={L} spinful Hubbard Trotter target ({len(g)} gates), {nl}-layer brickwall fit "
+                                  f"({nl * (L // 2)} gates), {what} over all 2^{L} columns",
+                      "real_parameters": 8 * nl * (L // 2) if a.config == "hess14" else 8 * nl,
+                      "L": L, "nlayers": nl, "target_gates": len(g)},
+           "s_per_eval": {"mixed": mx["s_per_eval"], "fp64": fp["s_per_eval"]},
+           "speedup_mixed_vs_fp64": fp["s_per_eval"] / mx["s_per_eval"], "accuracy": acc,
+           "extrapolated_from_sample": a.config == "grad18",
+           "sample_columns": min(a.sample_columns, ncols) if a.config == "grad18" else ncols}
+    print(json.dumps(out))
+
+
 def main():
     a = parse()
     if a.impl == "reference":
         run_reference(a)
+    elif a.config != "grad16":
+        run_secondary(a)
     else:
         run_gb300(a)
 

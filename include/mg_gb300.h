@@ -56,6 +56,11 @@ void mg_target_free(void* udata);
  * first use (about 2^(2L-1) amplitudes), so later evaluations against the same target
  * skip re-applying U.  Off by default. */
 int mg_target_set_resident(void* udata, int enable);
+/* Number of gates the GPU sweep of a circuit target applies per column: the circuit's
+ * gates less the fermionic swaps removed by relabelling wires (paired swaps that
+ * restore the qubit order; the other gates then carry Jordan-Wigner strings), plus
+ * any controlled-Z left over.  -1 for a dense target or an invalid handle. */
+int mg_target_sweep_gates(void* udata);
 
 /* ---------------------------------------------------------------------------------
  * Results the reference computes only inside larger calls

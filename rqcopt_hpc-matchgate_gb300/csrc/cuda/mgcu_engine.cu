@@ -1527,6 +1527,12 @@ extern "C" mgcu_target* mgcu_target_dense(const mgc* U, int L)
 }
 
 extern "C" void mgcu_target_destroy(mgcu_target* t) { delete t; }
+extern "C" int mgcu_target_sweep_gates(mgcu_target* t)
+{
+	if (t->kind != 0) return -1;
+	prepare_sweep(t);
+	return (int)t->sg.size();
+}
 extern "C" int mgcu_target_L(const mgcu_target* t) { return t->L; }
 extern "C" void mgcu_target_set_resident(mgcu_target* t, int enable)
 {

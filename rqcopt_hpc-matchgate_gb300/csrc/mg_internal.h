@@ -66,6 +66,7 @@ void mgcu_target_destroy(mgcu_target* t);
 int mgcu_target_apply(mgcu_target* t, const mgc* psi, mgc* out);      /* host vectors */
 int mgcu_target_L(const mgcu_target* t);
 void mgcu_target_set_resident(mgcu_target* t, int enable);
+int mgcu_target_sweep_gates(mgcu_target* t);
 
 /* ---- batched evaluation plans (the hot path) ---- */
 typedef struct

@@ -108,6 +108,7 @@ class MatchgateLib:
             L.mg_target_dense.argtypes = [P, C.c_int]
             L.mg_target_free.argtypes = [P]
             L.mg_target_set_resident.argtypes = [P, C.c_int]
+            L.mg_target_sweep_gates.argtypes = [P]
             L.mg_last_error.restype = C.c_char_p
             L.mg_plan_brickwall.argtypes = [P, P, P, C.c_int, C.c_int, P, C.c_int]
             L.mg_plan_set_gates.argtypes = [P, P]
