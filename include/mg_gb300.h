@@ -63,6 +63,31 @@ int mg_target_set_resident(void* udata, int enable);
 int mg_target_sweep_gates(void* udata);
 
 /* ---------------------------------------------------------------------------------
+ * Batches: f and the layer gradients of many independent brickwall fits at once, each
+ * against its own GPU circuit target (mg_target_circuit / mg_target_brickwall), any
+ * even qubit count and depth.  One persistent launch per phase covers every instance:
+ * columns are cut into work items of similar cost, taken largest first by all blocks,
+ * and the whole launch sequence is captured into a CUDA graph on the first run and
+ * replayed after.  Each instance's target tile size is chosen at creation by timing
+ * the candidates (2^10 .. 2^12 amplitudes) on a sample of its columns (tune != 0).
+ * Results equal those of one-instance evaluations up to summation order
+ * (deterministic from run to run).  Precision: the one set when the batch is created.
+ * --------------------------------------------------------------------------------- */
+typedef struct mg_batch mg_batch;
+mg_batch* mg_batch_create(int n, void* const targets[], const struct matchgate* const vlists[], const int nlayers[],
+                          const int* const* const perms[], const int nqubits[], int tune);
+int mg_batch_set_gates(mg_batch* batch, int i, const struct matchgate vlist[]);
+int mg_batch_run(mg_batch* batch);
+/* any output may be NULL: f, dvlist [nlayers_i] (as matchgate_brickwall_unitary_target_and_gradient),
+ * grad_vec [8 nlayers_i] (Riemannian, as the projected gradient) */
+int mg_batch_results(mg_batch* batch, int i, numeric* fval, struct matchgate dvlist[], double* grad_vec);
+/* the tuned target tile bits, the target's passes per column and the instance's work items */
+int mg_batch_info(mg_batch* batch, int i, int* target_tile_bits, int* target_passes, int* items);
+/* GPU time of `steps` graph replays (CUDA events), L2 flushed between them if asked */
+double mg_batch_time_ms(mg_batch* batch, int steps, int flush_l2);
+void mg_batch_free(mg_batch* batch);
+
+/* ---------------------------------------------------------------------------------
  * Results the reference computes only inside larger calls
  * --------------------------------------------------------------------------------- */
 

@@ -23,6 +23,7 @@
 #include <algorithm>
 #include <array>
 #include <map>
+#include <memory>
 #include <vector>
 
 namespace {
@@ -780,12 +781,12 @@ __device__ __forceinline__ void tgt_gates(char* tb, const TGate* gates, int gbeg
 	}
 }
 
-template <class P, int NT>
-__global__ void __launch_bounds__(NT, 512 / NT) k_target(Args<P> a)
+// -conj(U e_b) of one basis column b into out (the whole block)
+template <class P>
+__device__ __forceinline__ void tgt_column(const Args<P>& a, long b, typename P::T* out, char* smem_raw)
 {
 	typedef typename P::T T;
 	constexpr int ES = sizeof(T);
-	extern __shared__ __align__(16) char smem_raw[];
 	T* tile;
 	Smem s = smem_layout<T>(smem_raw, a.kt, tile);
 	char* tb = reinterpret_cast<char*>(tile);
@@ -793,11 +794,9 @@ __global__ void __launch_bounds__(NT, 512 / NT) k_target(Args<P> a)
 	const int kt = a.kt;
 	const unsigned n = 1u << kt, Q = n >> 2;
 	const int qpt = (Q == 4u * blockDim.x) ? 4 : (Q == 8u * blockDim.x) ? 8 : 0;
-	for (long b = a.b0 + blockIdx.x; b < a.b1; b += gridDim.x)
 	{
 		const int par = __popcll(b) & 1;
 		const unsigned cb = (unsigned)(b >> 1);
-		T* out = a.ucols + (size_t)(b - a.b0) * a.S;
 		for (int p = 0; p < a.U.npass; p++)
 		{
 			const PassRec& pr = a.U.pass[p];
@@ -849,38 +848,80 @@ __global__ void __launch_bounds__(NT, 512 / NT) k_target(Args<P> a)
 	}
 }
 
+template <class P, int NT>
+__global__ void __launch_bounds__(NT, 512 / NT) k_target(Args<P> a)
+{
+	extern __shared__ __align__(16) char smem_raw[];
+	for (long b = a.b0 + blockIdx.x; b < a.b1; b += gridDim.x)
+		tgt_column<P>(a, b, a.ucols + (size_t)(b - a.b0) * a.S, smem_raw);
+}
+
+// ------------------------------------------------------------------------------------
+// batched launches: work items (instance, column range) of many instances, taken by
+// persistent blocks from an atomic counter in the order given (largest first); each
+// item writes its own partial rows, so results do not depend on which block ran it
+// ------------------------------------------------------------------------------------
+struct BatchItem
+{
+	int inst;      // instance
+	int slot;      // the item's partial row in its instance's part_f / part_g
+	long b0, b1;   // columns
+	long stage;    // element offset of column b0's target column in the staging buffer
+};
+
+__device__ __forceinline__ int next_item(int* counter, int* shared_slot)
+{
+	if (threadIdx.x == 0) *shared_slot = atomicAdd(counter, 1);
+	__syncthreads();
+	const int it = *shared_slot;
+	__syncthreads();
+	return it;
+}
+
+template <class P>
+__global__ void __launch_bounds__(256, 2) k_target_batch(const Args<P>* __restrict__ args, const BatchItem* __restrict__ items,
+	int nitems, int* counter, typename P::T* stage)
+{
+	extern __shared__ __align__(16) char smem_raw[];
+	__shared__ int it_s;
+	for (;;)
+	{
+		const int it = next_item(counter, &it_s);
+		if (it >= nitems) break;
+		const BatchItem I = items[it];
+		const Args<P>& a = args[I.inst];
+		for (long b = I.b0; b < I.b1; b++) tgt_column<P>(a, b, stage + I.stage + (size_t)(b - I.b0) * a.S, smem_raw);
+	}
+}
+
 // ------------------------------------------------------------------------------------
 // stage A: per column -- W forward with cache, overlap, W backward; the target column
 // comes from `dense` (k_target's output, a dense or host target) or, with WithU, from
 // a sweep of the target program inside this kernel
 // ------------------------------------------------------------------------------------
+// one basis column b: target column from dense (or, WithU and no dense, the target
+// program run into su), forward W with gate-input cache, overlap into facc, backward
+// with gradient rows added to part_g row prow.  su, sw: the block's column slots;
+// cache / dcache: this column's gate caches (null: none)
 template <class P, bool WithU>
-__global__ void __launch_bounds__(256) k_columns(Args<P> a)
+__device__ __forceinline__ void w_column(const Args<P>& a, long b, const typename P::T* dense, long dense_b0, long prow,
+	typename P::T* su, typename P::T* sw, typename P::T* cache, typename P::T* dcache, typename P::Acc& facc, char* smem_raw)
 {
 	typedef typename P::T T;
-	extern __shared__ __align__(16) char smem_raw[];
 	T* tile;
 	Smem s = smem_layout<T>(smem_raw, a.kt, tile);
 	const int kt = a.kt, Q = 1 << (kt - 2);
 	const long S = a.S;
-	typename P::Acc facc = P::acc_zero();
-	T* su = a.su + (size_t)blockIdx.x * S;
-	T* sw = a.sw + (size_t)blockIdx.x * S;
-
-	for (long b = a.b0 + blockIdx.x; b < a.b1; b += gridDim.x)
 	{
 		const int par = __popcll(b) & 1;
 		const unsigned cb = (unsigned)(b >> 1);
 		const T* dsrc;
-		if (!WithU || a.dense) dsrc = a.dense + (size_t)(b - a.dense_b0) * S;
+		if (!WithU || dense) dsrc = dense + (size_t)(b - dense_b0) * S;
 		else
 		{
 			run_forward<P>(a.U, a.um, kt, a.nb, par, cb, tile, s, su, true, a.ukind);
 			dsrc = su;
 		}
-		const long slot = a.cache_per_column ? (b - a.b0) : blockIdx.x;
-		T* cache = a.cache ? a.cache + (size_t)slot * a.ngates * S : nullptr;
-		T* dcache = a.dcache ? a.dcache + (size_t)slot * a.ngates * S : nullptr;
 
 		// W forward, caching each gate's input; overlap on the last pass
 		for (int p = 0; p < a.W.npass; p++)
@@ -915,7 +956,7 @@ __global__ void __launch_bounds__(256) k_columns(Args<P> a)
 			}
 		}
 
-		if (!a.want_grad) continue;
+		if (!a.want_grad) return;
 
 		// W backward: tile holds the derivative after the gate
 		for (int p = a.W.npass - 1; p >= 0; p--)
@@ -954,14 +995,61 @@ __global__ void __launch_bounds__(256) k_columns(Args<P> a)
 						tile[ey] = P::madd2(G.c0, dy, G.c2, dz);
 						tile[ez] = P::madd2(G.c1, dy, G.c3, dz);
 					}
-					block_reduce8<P>(acc, s.red, a.part_g + ((size_t)blockIdx.x * a.ngates + r.g) * 16, 1.0);
+					block_reduce8<P>(acc, s.red, a.part_g + ((size_t)prow * a.ngates + r.g) * 16, 1.0);
 				}
 				if (p > 0) tile_store<P>(tile, kt, s, nlb, su, false);
 				__syncthreads();
 			}
 		}
 	}
+}
+
+template <class P, bool WithU>
+__global__ void __launch_bounds__(256) k_columns(Args<P> a)
+{
+	typedef typename P::T T;
+	extern __shared__ __align__(16) char smem_raw[];
+	const long S = a.S;
+	typename P::Acc facc = P::acc_zero();
+	T* su = a.su + (size_t)blockIdx.x * S;
+	T* sw = a.sw + (size_t)blockIdx.x * S;
+	for (long b = a.b0 + blockIdx.x; b < a.b1; b += gridDim.x)
+	{
+		const long slot = a.cache_per_column ? (b - a.b0) : blockIdx.x;
+		T* cache = a.cache ? a.cache + (size_t)slot * a.ngates * S : nullptr;
+		T* dcache = a.dcache ? a.dcache + (size_t)slot * a.ngates * S : nullptr;
+		w_column<P, WithU>(a, b, a.dense, a.dense_b0, blockIdx.x, su, sw, cache, dcache, facc, smem_raw);
+	}
+	T* tile;
+	Smem s = smem_layout<T>(smem_raw, a.kt, tile);
 	block_reduce1<P>(facc, s.red, a.part_f + (size_t)blockIdx.x * 2);
+}
+
+// batched gradient items: target columns staged by k_target_batch; the block's slots and
+// gate cache live in per-block scratch (stride slot_stride / cache_stride elements)
+template <class P>
+__global__ void __launch_bounds__(256) k_columns_batch(const Args<P>* __restrict__ args, const BatchItem* __restrict__ items,
+	int nitems, int* counter, const typename P::T* stage, typename P::T* scratch, long slot_stride, long cache_stride)
+{
+	typedef typename P::T T;
+	extern __shared__ __align__(16) char smem_raw[];
+	__shared__ int it_s;
+	T* su = scratch + (size_t)blockIdx.x * (2 * slot_stride + cache_stride);
+	T* sw = su + slot_stride;
+	T* cache = sw + slot_stride;
+	for (;;)
+	{
+		const int it = next_item(counter, &it_s);
+		if (it >= nitems) break;
+		const BatchItem I = items[it];
+		const Args<P>& a = args[I.inst];
+		typename P::Acc facc = P::acc_zero();
+		for (long b = I.b0; b < I.b1; b++)
+			w_column<P, false>(a, b, stage + I.stage, I.b0, I.slot, su, sw, a.want_grad ? cache : nullptr, nullptr, facc, smem_raw);
+		T* tile;
+		Smem s = smem_layout<T>(smem_raw, a.kt, tile);
+		block_reduce1<P>(facc, s.red, a.part_f + (size_t)I.slot * 2);
+	}
 }
 
 // ------------------------------------------------------------------------------------
@@ -1349,10 +1437,8 @@ static int upload_sched(const Sched& s, DevBuf& pass, DevBuf& gate)
 }
 
 template <class P>
-static int target_prog(mgcu_target* t, int kt, int threads, TargetProg*& out)
+static int build_target_prog(mgcu_target* t, int kt, int threads, TargetProg& tp)
 {
-	TargetProg& tp = t->progs[P::kId];
-	if (tp.kt != kt || tp.threads != threads)
 	{
 		typedef typename P::T T;
 		prepare_sweep(t);
@@ -1495,6 +1581,19 @@ static int target_prog(mgcu_target* t, int kt, int threads, TargetProg*& out)
 		MGCU_TRY(cudaMemcpy(tp.pm.p, pmh.data(), sizeof(int2) * pmh.size(), cudaMemcpyHostToDevice));
 		tp.kt = kt;
 		tp.threads = threads;
+	}
+	return 0;
+}
+
+// the target's cached program for this precision, rebuilt when the tile or block size changes
+template <class P>
+static int target_prog(mgcu_target* t, int kt, int threads, TargetProg*& out)
+{
+	TargetProg& tp = t->progs[P::kId];
+	if (tp.kt != kt || tp.threads != threads)
+	{
+		const int e = build_target_prog<P>(t, kt, threads, tp);
+		if (e) { tp.kt = -1; return e; }
 	}
 	out = &tp;
 	return 0;
@@ -1968,6 +2067,420 @@ extern "C" int mgcu_plan_target_kernel_ms(mgcu_plan* p, double* ms, long* launch
 	*ms = t;
 	*launches = (long)(p->kev_used / 2);
 	return 0;
+}
+
+// ======================================================================================
+// Batches: many independent instances (brickwall fits against GPU circuit targets of
+// any qubit count and depth), f and block gradients, in one persistent launch per phase
+// and round; the launch sequence is captured once into a CUDA graph and replayed.
+// ======================================================================================
+namespace {
+
+// fixed-order sums of one instance's item rows (one block per instance)
+struct BatchRed
+{
+	const double* part_f;   // [nslots][2]
+	const double* part_g;   // [nslots][ngates][16]
+	const int* block;       // [ngates]
+	double* out_f;          // [2]
+	double* out_blk;        // [nblocks][16]
+	int nslots, ngates, nblocks;
+};
+
+__global__ void k_batch_reduce(const BatchRed* __restrict__ rd)
+{
+	const BatchRed r = rd[blockIdx.x];
+	if (threadIdx.x < 2)
+	{
+		double s = 0;
+		for (int k = 0; k < r.nslots; k++) s += r.part_f[2 * k + threadIdx.x];
+		r.out_f[threadIdx.x] = s;
+	}
+	for (int q = threadIdx.x; q < r.nblocks * 16; q += blockDim.x)
+	{
+		const int blk = q >> 4, e = q & 15;
+		double s = 0;
+		for (int g = 0; g < r.ngates; g++)
+		{
+			if (r.block[g] != blk) continue;
+			for (int k = 0; k < r.nslots; k++) s += r.part_g[((size_t)k * r.ngates + g) * 16 + e];
+		}
+		r.out_blk[q] = s;
+	}
+}
+
+struct BatchInst
+{
+	int L, nb, ngates, nblocks, kt_c, kt_t, nslots = 0, npass_t = 0;
+	long S;
+	Sched ws;
+	std::vector<int> block;
+	DevBuf d_pass, d_gate, d_mats, d_block, out_f, out_blk;
+	TargetProg tp;                 // the batch's own copy of the target program
+	mgcu_target* target;
+	size_t smem_t, pm_off, smem_c;
+	double col_cost;               // relative cost of one column
+	long part_off;                 // offsets (doubles) of part_f / part_g in the batch's partials
+	long part_g_off;
+};
+
+} // namespace
+
+struct mgcu_batch
+{
+	int prec, n, threads = 256;
+	size_t tsize;
+	std::unique_ptr<BatchInst[]> inst;
+	DevBuf args_t, args_c, items, counters, stage, scratch, parts, red;
+	std::vector<int> round_beg;    // item index where each round starts (plus the end)
+	long slot_stride = 0, cache_stride = 0;
+	size_t smem_t = 0, smem_c = 0;
+	int grid_t = 0, grid_c = 0, nitems = 0;
+	long graph_kernels = 0;        // kernel nodes per replay
+	cudaGraph_t graph = nullptr;
+	cudaGraphExec_t exec = nullptr;
+	DevBuf flush;
+	~mgcu_batch()
+	{
+		if (exec) cudaGraphExecDestroy(exec);
+		if (graph) cudaGraphDestroy(graph);
+	}
+};
+
+namespace {
+
+template <class P>
+static size_t target_smem(int kt, int threads, size_t tsize, size_t& pm_off)
+{
+	pm_off = ((size_t)1 << kt) * tsize + 2 * 128 * sizeof(unsigned) + std::max<size_t>((size_t)(threads / 32) * 16 * sizeof(double), 16 * 16);
+	return pm_off + (size_t)MAXPM * 8 * tsize;
+}
+
+// Time the target sweep of t with tile bits kt on ncols columns (ms), using a temporary
+// program and output buffer; used to choose each instance's tile size.
+template <class P>
+static double time_target(mgcu_target* t, int L, int kt, int threads, long ncols, int grid_cap)
+{
+	typedef typename P::T T;
+	MgcuContext* c = mgcu_ctx();
+	TargetProg tp;
+	if (build_target_prog<P>(t, kt, threads, tp)) return -1;
+	size_t pm_off;
+	const size_t smem = target_smem<P>(kt, threads, sizeof(T), pm_off);
+	DevBuf out;
+	const long S = 1L << (L - 1);
+	if (out.alloc(sizeof(T) * S * ncols)) return -1;
+	Args<P> a;
+	memset(&a, 0, sizeof(a));
+	a.L = L; a.nb = L - 1; a.kt = kt; a.S = S;
+	a.U.pass = tp.pass.as<PassRec>(); a.U.gate = tp.gate.as<GateRec>(); a.U.npass = (int)tp.sched.pass.size();
+	a.utg = tp.tg.as<TGate>(); a.upm = tp.pm.as<int2>(); a.upmats = tp.pmats.as<T>(); a.pm_off = (unsigned)pm_off;
+	a.b0 = 0; a.b1 = ncols; a.ucols = out.as<T>();
+	int per_sm = 0;
+	if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_target<P, 256>, threads, smem) != cudaSuccess || per_sm < 1) return -1;
+	const int grid = (int)std::min<long>(std::min<long>((long)c->nsm * per_sm, grid_cap), ncols);
+	double best = -1;
+	for (int rep = 0; rep < 2; rep++)
+	{
+		cudaEventRecord(c->ev0, c->stream);
+		k_target<P, 256><<<grid, threads, smem, c->stream>>>(a);
+		cudaEventRecord(c->ev1, c->stream);
+		if (cudaEventSynchronize(c->ev1) != cudaSuccess) return -1;
+		float ms = 0;
+		cudaEventElapsedTime(&ms, c->ev0, c->ev1);
+		if (rep == 1) best = ms;   // the first run warms caches and code
+	}
+	return best;
+}
+
+template <class P>
+static int batch_build(mgcu_batch* B, const mgcu_batch_inst* d, int tune)
+{
+	typedef typename P::T T;
+	MgcuContext* c = mgcu_ctx();
+	const int threads = B->threads;
+	MGCU_TRY(cudaFuncSetAttribute(k_target<P, 256>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)std::min<size_t>(c->smem_optin, 227 * 1024)));
+	const int kt_default = sizeof(T) >= 16 ? 12 : 13;
+	// tile choice per distinct (target, L): time the candidates on a column sample
+	std::map<std::pair<mgcu_target*, int>, int> tuned;
+	for (int i = 0; i < B->n; i++)
+	{
+		BatchInst& I = B->inst[i];
+		const mgcu_batch_inst& D = d[i];
+		I.L = D.L; I.nb = D.L - 1; I.S = 1L << (D.L - 1); I.ngates = D.ngates; I.nblocks = D.nblocks; I.target = D.target;
+		I.block.assign(D.block, D.block + D.ngates);
+		I.kt_c = std::min(kt_default, I.nb);
+		const std::pair<mgcu_target*, int> key(D.target, D.L);
+		auto it = tuned.find(key);
+		if (it == tuned.end())
+		{
+			int best_kt = std::min(kt_default, I.nb);
+			if (tune && I.nb > 10)
+			{
+				double best_ms = -1;
+				const long ncols = std::min<long>(1L << D.L, (long)c->nsm * 4);
+				for (int kt = 10; kt <= std::min(kt_default, I.nb); kt++)
+				{
+					const double ms = time_target<P>(D.target, D.L, kt, threads, ncols, c->nsm * 2);
+					if (ms > 0 && (best_ms < 0 || ms < best_ms)) { best_ms = ms; best_kt = kt; }
+				}
+			}
+			it = tuned.emplace(key, best_kt).first;
+		}
+		I.kt_t = it->second;
+		int e = build_target_prog<P>(D.target, I.kt_t, threads, I.tp);
+		if (e) return e;
+		I.npass_t = (int)I.tp.sched.pass.size();
+		I.smem_t = target_smem<P>(I.kt_t, threads, sizeof(T), I.pm_off);
+		I.smem_c = ((size_t)1 << I.kt_c) * sizeof(T) + 2 * 128 * sizeof(unsigned) + (size_t)(threads / 32) * 16 * sizeof(double);
+		schedule(I.L, I.kt_c, D.wires, D.ngates, false, I.ws);
+		e = upload_sched(I.ws, I.d_pass, I.d_gate);
+		if (!e) e = I.d_mats.alloc(sizeof(T) * 8 * std::max(D.ngates, 1));
+		if (!e) e = I.d_block.alloc(sizeof(int) * std::max(D.ngates, 1));
+		if (!e) e = I.out_f.alloc(sizeof(double) * 2);
+		if (!e) e = I.out_blk.alloc(sizeof(double) * 16 * std::max(D.nblocks, 1));
+		if (e) return e;
+		MGCU_TRY(cudaMemcpy(I.d_block.p, D.block, sizeof(int) * D.ngates, cudaMemcpyHostToDevice));
+		I.col_cost = (double)I.S * ((double)mgcu_target_sweep_gates(D.target) + 3.0 * D.ngates);
+		B->smem_t = std::max(B->smem_t, I.smem_t);
+		B->smem_c = std::max(B->smem_c, I.smem_c);
+		B->slot_stride = std::max(B->slot_stride, I.S);
+		B->cache_stride = std::max(B->cache_stride, I.S * D.ngates);
+	}
+	// the batched kernels also hold one static shared int: ask for exactly what they use
+	MGCU_TRY(cudaFuncSetAttribute(k_target_batch<P>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)B->smem_t));
+	MGCU_TRY(cudaFuncSetAttribute(k_columns_batch<P>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)B->smem_c));
+	int pt = 0, pc = 0;
+	MGCU_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&pt, k_target_batch<P>, threads, B->smem_t));
+	MGCU_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&pc, k_columns_batch<P>, threads, B->smem_c));
+	if (pt < 1 || pc < 1) { mg_set_error("batch: a block does not fit on an SM"); return MG_ERR_ARG; }
+	B->grid_t = c->nsm * pt;
+	B->grid_c = c->nsm * pc;
+
+	// work items: about 16 per block, never more than an instance's columns, largest first
+	double total = 0;
+	for (int i = 0; i < B->n; i++) total += B->inst[i].col_cost * (double)(1L << B->inst[i].L);
+	const double item_cost = total / (16.0 * std::max(B->grid_t, B->grid_c));
+	struct HostItem { BatchItem it; double cost; };
+	std::vector<HostItem> all;
+	for (int i = 0; i < B->n; i++)
+	{
+		BatchInst& I = B->inst[i];
+		const long N = 1L << I.L;
+		const long per = std::max(1L, std::min(N, (long)(item_cost / I.col_cost)));
+		for (long b0 = 0; b0 < N; b0 += per)
+		{
+			HostItem h;
+			h.it.inst = i; h.it.slot = I.nslots++; h.it.b0 = b0; h.it.b1 = std::min(N, b0 + per); h.it.stage = 0;
+			h.cost = I.col_cost * (double)(h.it.b1 - h.it.b0);
+			all.push_back(h);
+		}
+	}
+	std::stable_sort(all.begin(), all.end(), [](const HostItem& x, const HostItem& y) { return x.cost > y.cost; });
+	// rounds: staged target columns of a round within 16 GB
+	const size_t budget = 16ull << 30;
+	std::vector<BatchItem> items;
+	size_t used = 0, max_used = 0;
+	B->round_beg.assign(1, 0);
+	for (HostItem& h : all)
+	{
+		const size_t bytes = sizeof(T) * (size_t)B->inst[h.it.inst].S * (size_t)(h.it.b1 - h.it.b0);
+		if (used + bytes > budget && used > 0) { B->round_beg.push_back((int)items.size()); used = 0; }
+		h.it.stage = (long)(used / sizeof(T));
+		used += bytes;
+		max_used = std::max(max_used, used);
+		items.push_back(h.it);
+	}
+	B->round_beg.push_back((int)items.size());
+	B->nitems = (int)items.size();
+
+	// partial rows of every instance in one buffer
+	long off = 0;
+	for (int i = 0; i < B->n; i++)
+	{
+		BatchInst& I = B->inst[i];
+		I.part_off = off; off += 2L * I.nslots;
+		I.part_g_off = off; off += 16L * I.nslots * std::max(I.ngates, 1);
+	}
+	const int nrounds = (int)B->round_beg.size() - 1;
+	int e = B->parts.alloc(sizeof(double) * std::max(off, 1L));
+	if (!e) e = B->stage.alloc(std::max<size_t>(max_used, 16));
+	if (!e) e = B->scratch.alloc(sizeof(T) * (size_t)B->grid_c * (size_t)(2 * B->slot_stride + B->cache_stride));
+	if (!e) e = B->items.alloc(sizeof(BatchItem) * std::max<size_t>(items.size(), 1));
+	if (!e) e = B->counters.alloc(sizeof(int) * 2 * std::max(nrounds, 1));
+	if (!e) e = B->args_t.alloc(sizeof(Args<P>) * B->n);
+	if (!e) e = B->args_c.alloc(sizeof(Args<P>) * B->n);
+	if (!e) e = B->red.alloc(sizeof(BatchRed) * B->n);
+	if (e) return e;
+	MGCU_TRY(cudaMemcpy(B->items.p, items.data(), sizeof(BatchItem) * items.size(), cudaMemcpyHostToDevice));
+	std::vector<Args<P>> at(B->n), ac(B->n);
+	std::vector<BatchRed> rd(B->n);
+	double* parts = B->parts.as<double>();
+	for (int i = 0; i < B->n; i++)
+	{
+		BatchInst& I = B->inst[i];
+		Args<P>& a = at[i];
+		memset(&a, 0, sizeof(a));
+		a.L = I.L; a.nb = I.nb; a.kt = I.kt_t; a.S = I.S;
+		a.U.pass = I.tp.pass.as<PassRec>(); a.U.gate = I.tp.gate.as<GateRec>(); a.U.npass = (int)I.tp.sched.pass.size();
+		a.utg = I.tp.tg.as<TGate>(); a.upm = I.tp.pm.as<int2>(); a.upmats = I.tp.pmats.as<T>(); a.pm_off = (unsigned)I.pm_off;
+		Args<P>& w = ac[i];
+		memset(&w, 0, sizeof(w));
+		w.L = I.L; w.nb = I.nb; w.kt = I.kt_c; w.S = I.S;
+		w.W.pass = I.d_pass.as<PassRec>(); w.W.gate = I.d_gate.as<GateRec>(); w.W.npass = (int)I.ws.pass.size();
+		w.wm = I.d_mats.as<T>(); w.ngates = I.ngates; w.want_grad = 1;
+		w.part_f = parts + I.part_off; w.part_g = parts + I.part_g_off;
+		BatchRed& r = rd[i];
+		r.part_f = parts + I.part_off; r.part_g = parts + I.part_g_off; r.block = I.d_block.as<int>();
+		r.out_f = I.out_f.as<double>(); r.out_blk = I.out_blk.as<double>();
+		r.nslots = I.nslots; r.ngates = I.ngates; r.nblocks = I.nblocks;
+	}
+	MGCU_TRY(cudaMemcpy(B->args_t.p, at.data(), sizeof(Args<P>) * B->n, cudaMemcpyHostToDevice));
+	MGCU_TRY(cudaMemcpy(B->args_c.p, ac.data(), sizeof(Args<P>) * B->n, cudaMemcpyHostToDevice));
+	MGCU_TRY(cudaMemcpy(B->red.p, rd.data(), sizeof(BatchRed) * B->n, cudaMemcpyHostToDevice));
+	return 0;
+}
+
+// the launch sequence of one batch evaluation on the library's stream
+template <class P>
+static int batch_issue(mgcu_batch* B)
+{
+	typedef typename P::T T;
+	cudaStream_t st = mgcu_ctx()->stream;
+	const int nrounds = (int)B->round_beg.size() - 1;
+	MGCU_TRY(cudaMemsetAsync(B->parts.p, 0, B->parts.n, st));
+	MGCU_TRY(cudaMemsetAsync(B->counters.p, 0, B->counters.n, st));
+	for (int r = 0; r < nrounds; r++)
+	{
+		const int i0 = B->round_beg[r], ni = B->round_beg[r + 1] - i0;
+		const BatchItem* items = B->items.as<BatchItem>() + i0;
+		int* ctr = B->counters.as<int>() + 2 * r;
+		k_target_batch<P><<<std::min(B->grid_t, ni), B->threads, B->smem_t, st>>>(B->args_t.as<Args<P>>(), items, ni, ctr, B->stage.as<T>());
+		MGCU_LAUNCHED();
+		k_columns_batch<P><<<std::min(B->grid_c, ni), B->threads, B->smem_c, st>>>(B->args_c.as<Args<P>>(), items, ni, ctr + 1,
+			B->stage.as<T>(), B->scratch.as<T>(), B->slot_stride, B->cache_stride);
+		MGCU_LAUNCHED();
+	}
+	k_batch_reduce<<<B->n, 128, 0, st>>>(B->red.as<BatchRed>());
+	MGCU_LAUNCHED();
+	return 0;
+}
+
+template <class P>
+static int batch_issue_graph(mgcu_batch* B)
+{
+	cudaStream_t st = mgcu_ctx()->stream;
+	if (!B->exec)
+	{
+		MGCU_TRY(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
+		const long n0 = mgcu_launch_count();
+		const int e = batch_issue<P>(B);
+		B->graph_kernels = mgcu_launch_count() - n0;
+		mgcu_count_launch(-B->graph_kernels);   // counted when the graph runs
+		cudaGraph_t g = nullptr;
+		const cudaError_t ce = cudaStreamEndCapture(st, &g);
+		if (e || ce != cudaSuccess) { if (g) cudaGraphDestroy(g); if (!e) MGCU_TRY(ce); return e ? e : MG_ERR_DEVICE; }
+		B->graph = g;
+		MGCU_TRY(cudaGraphInstantiate(&B->exec, B->graph, 0));
+	}
+	MGCU_TRY(cudaGraphLaunch(B->exec, st));
+	mgcu_count_launch(B->graph_kernels);
+	return 0;
+}
+
+} // namespace
+
+extern "C" mgcu_batch* mgcu_batch_create(int n, const mgcu_batch_inst* d, int precision, int tune)
+{
+	if (!mgcu_ctx()) return nullptr;
+	if (n < 1) { mg_set_error("a batch needs at least one instance"); return nullptr; }
+	for (int i = 0; i < n; i++)
+		if (!d[i].target || d[i].target->kind != 0 || d[i].target->L != d[i].L || d[i].L < 4 || d[i].L > 30 || d[i].ngates < 1)
+		{
+			mg_set_error("batch instance %d: needs a GPU circuit target on its qubits (4..30) and at least one gate", i);
+			return nullptr;
+		}
+	mgcu_batch* B = new mgcu_batch();
+	B->prec = precision; B->n = n; B->tsize = prec_tsize(precision);
+	B->inst.reset(new BatchInst[n]);
+	int e;
+	if (precision == MG_PREC_FP64_ID) e = batch_build<PrecD>(B, d, tune);
+	else if (precision == MG_PREC_FP32_ID) e = batch_build<PrecF>(B, d, tune);
+	else e = batch_build<PrecX>(B, d, tune);
+	if (e) { delete B; return nullptr; }
+	return B;
+}
+
+extern "C" void mgcu_batch_destroy(mgcu_batch* B) { delete B; }
+
+extern "C" int mgcu_batch_set_gates(mgcu_batch* B, int i, const mgg* gates)
+{
+	if (i < 0 || i >= B->n) { mg_set_error("batch instance %d out of range", i); return MG_ERR_ARG; }
+	BatchInst& I = B->inst[i];
+	if (B->prec == MG_PREC_FP64_ID) return upload_mats<PrecD>(gates, I.ngates, I.d_mats);
+	if (B->prec == MG_PREC_FP32_ID) return upload_mats<PrecF>(gates, I.ngates, I.d_mats);
+	return upload_mats<PrecX>(gates, I.ngates, I.d_mats);
+}
+
+// one evaluation of every instance (graph replay; the first call captures the graph)
+extern "C" int mgcu_batch_run(mgcu_batch* B)
+{
+	int e;
+	if (B->prec == MG_PREC_FP64_ID) e = batch_issue_graph<PrecD>(B);
+	else if (B->prec == MG_PREC_FP32_ID) e = batch_issue_graph<PrecF>(B);
+	else e = batch_issue_graph<PrecX>(B);
+	if (e) return e;
+	MGCU_TRY(cudaStreamSynchronize(mgcu_ctx()->stream));
+	return 0;
+}
+
+extern "C" int mgcu_batch_fetch(mgcu_batch* B, int i, mgc* f, mgg* dblocks)
+{
+	if (i < 0 || i >= B->n) { mg_set_error("batch instance %d out of range", i); return MG_ERR_ARG; }
+	BatchInst& I = B->inst[i];
+	if (f) MGCU_TRY(cudaMemcpy(f, I.out_f.p, sizeof(double) * 2, cudaMemcpyDeviceToHost));
+	if (dblocks) MGCU_TRY(cudaMemcpy(dblocks, I.out_blk.p, sizeof(double) * 16 * I.nblocks, cudaMemcpyDeviceToHost));
+	return 0;
+}
+
+extern "C" int mgcu_batch_project(mgcu_batch* B, int i, const mgg* vblocks, double* grad_vec)
+{
+	if (i < 0 || i >= B->n) { mg_set_error("batch instance %d out of range", i); return MG_ERR_ARG; }
+	BatchInst& I = B->inst[i];
+	return mgcu_project_dev(vblocks, I.nblocks, I.out_blk.as<double>(), nullptr, grad_vec, nullptr);
+}
+
+extern "C" int mgcu_batch_info(const mgcu_batch* B, int i, int* target_tile_bits, int* target_passes, int* items)
+{
+	if (i < 0 || i >= B->n) { mg_set_error("batch instance %d out of range", i); return MG_ERR_ARG; }
+	const BatchInst& I = B->inst[i];
+	if (target_tile_bits) *target_tile_bits = I.kt_t;
+	if (target_passes) *target_passes = I.npass_t;
+	if (items) *items = I.nslots;
+	return 0;
+}
+
+extern "C" double mgcu_batch_time_ms(mgcu_batch* B, int steps, int flush_l2)
+{
+	MgcuContext* c = mgcu_ctx();
+	if (flush_l2 && B->flush.alloc(512ull << 20)) return -1;
+	double total = 0;
+	for (int s = 0; s < steps; s++)
+	{
+		if (flush_l2 && cudaMemsetAsync(B->flush.p, s & 0xff, B->flush.n, c->stream) != cudaSuccess) return -1;
+		cudaEventRecord(c->ev0, c->stream);
+		int e;
+		if (B->prec == MG_PREC_FP64_ID) e = batch_issue_graph<PrecD>(B);
+		else if (B->prec == MG_PREC_FP32_ID) e = batch_issue_graph<PrecF>(B);
+		else e = batch_issue_graph<PrecX>(B);
+		if (e) return -1;
+		cudaEventRecord(c->ev1, c->stream);
+		if (cudaEventSynchronize(c->ev1) != cudaSuccess) return -1;
+		float ms = 0;
+		cudaEventElapsedTime(&ms, c->ev0, c->ev1);
+		total += ms;
+	}
+	return total;
 }
 
 // ======================================================================================

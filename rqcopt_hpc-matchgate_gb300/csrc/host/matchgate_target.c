@@ -628,3 +628,118 @@ int mg_plan_target_kernel_ms(mg_plan* pl, double* ms, long* launches)
 	mgcu_unlock();
 	return e ? MG_ERR_DEVICE : 0;
 }
+
+/* ======================================================================================
+ * batches
+ * ====================================================================================== */
+struct mg_batch
+{
+	mgcu_batch* b;
+	int n;
+	int* nlayers;
+	int* L;
+	seq_circuit* s;
+	struct matchgate** vlist;
+};
+
+void mg_batch_free(mg_batch* bt)
+{
+	if (!bt) return;
+	if (bt->b) { mgcu_lock(); mgcu_batch_destroy(bt->b); mgcu_unlock(); }
+	for (int i = 0; i < bt->n; i++)
+	{
+		if (bt->s) seq_free(&bt->s[i]);
+		if (bt->vlist) free(bt->vlist[i]);
+	}
+	free(bt->s); free(bt->vlist); free(bt->nlayers); free(bt->L);
+	free(bt);
+}
+
+mg_batch* mg_batch_create(int n, void* const targets[], const struct matchgate* const vlists[], const int nlayers[],
+	const int* const* const perms[], const int nqubits[], int tune)
+{
+	if (n < 1 || !targets || !vlists || !nlayers || !perms || !nqubits) { mg_set_error("mg_batch_create: bad arguments"); return NULL; }
+	mg_batch* bt = calloc(1, sizeof(*bt));
+	if (!bt) return NULL;
+	bt->n = n;
+	bt->nlayers = malloc(sizeof(int) * n); bt->L = malloc(sizeof(int) * n);
+	bt->s = calloc(n, sizeof(seq_circuit)); bt->vlist = calloc(n, sizeof(struct matchgate*));
+	mgcu_batch_inst* d = calloc(n, sizeof(mgcu_batch_inst));
+	if (!bt->nlayers || !bt->L || !bt->s || !bt->vlist || !d) { free(d); mg_batch_free(bt); return NULL; }
+	for (int i = 0; i < n; i++)
+	{
+		mg_target_handle* th = (mg_target_handle*)targets[i];
+		if (!th || th->magic != MG_TARGET_MAGIC || th->L != nqubits[i])
+		{
+			mg_set_error("mg_batch_create: instance %d needs a GPU target (mg_target_*) on its qubits", i);
+			free(d); mg_batch_free(bt); return NULL;
+		}
+		if (brickwall_seq(vlists[i], nlayers[i], nqubits[i], (const int**)perms[i], &bt->s[i])) { free(d); mg_batch_free(bt); return NULL; }
+		bt->nlayers[i] = nlayers[i]; bt->L[i] = nqubits[i];
+		bt->vlist[i] = malloc(sizeof(struct matchgate) * nlayers[i]);
+		if (!bt->vlist[i]) { free(d); mg_batch_free(bt); return NULL; }
+		memcpy(bt->vlist[i], vlists[i], sizeof(struct matchgate) * nlayers[i]);
+		d[i].target = th->dev; d[i].L = nqubits[i]; d[i].ngates = bt->s[i].ngates; d[i].wires = bt->s[i].wires;
+		d[i].nblocks = nlayers[i]; d[i].block = bt->s[i].block;
+	}
+	mgcu_lock();
+	bt->b = mgcu_batch_create(n, d, mgcu_precision(), tune);
+	int r = bt->b ? 0 : MG_ERR_DEVICE;
+	for (int i = 0; i < n && !r; i++) r = mgcu_batch_set_gates(bt->b, i, (const mgg*)bt->s[i].gates);
+	mgcu_unlock();
+	free(d);
+	if (r) { mg_batch_free(bt); return NULL; }
+	return bt;
+}
+
+int mg_batch_set_gates(mg_batch* bt, int i, const struct matchgate vlist[])
+{
+	if (!bt || i < 0 || i >= bt->n) { mg_set_error("mg_batch_set_gates: bad instance %d", i); return MG_ERR_ARG; }
+	const int half = bt->L[i] / 2;
+	memcpy(bt->vlist[i], vlist, sizeof(struct matchgate) * bt->nlayers[i]);
+	for (int l = 0; l < bt->nlayers[i]; l++)
+		for (int p = 0; p < half; p++) bt->s[i].gates[l * half + p] = vlist[l];
+	mgcu_lock();
+	int r = mgcu_batch_set_gates(bt->b, i, (const mgg*)bt->s[i].gates);
+	mgcu_unlock();
+	return r;
+}
+
+int mg_batch_run(mg_batch* bt)
+{
+	if (!bt) return MG_ERR_ARG;
+	mgcu_lock();
+	int r = mgcu_batch_run(bt->b);
+	mgcu_unlock();
+	return r;
+}
+
+int mg_batch_results(mg_batch* bt, int i, numeric* fval, struct matchgate dvlist[], double* grad_vec)
+{
+	if (!bt || i < 0 || i >= bt->n) { mg_set_error("mg_batch_results: bad instance %d", i); return MG_ERR_ARG; }
+	mgcu_lock();
+	mgc f;
+	int r = mgcu_batch_fetch(bt->b, i, &f, (mgg*)dvlist);
+	if (!r && grad_vec) r = mgcu_batch_project(bt->b, i, (const mgg*)bt->vlist[i], grad_vec);
+	mgcu_unlock();
+	if (!r && fval) *fval = f.re + I * f.im;
+	return r;
+}
+
+int mg_batch_info(mg_batch* bt, int i, int* target_tile_bits, int* target_passes, int* items)
+{
+	if (!bt) return MG_ERR_ARG;
+	mgcu_lock();
+	int r = mgcu_batch_info(bt->b, i, target_tile_bits, target_passes, items);
+	mgcu_unlock();
+	return r;
+}
+
+double mg_batch_time_ms(mg_batch* bt, int steps, int flush_l2)
+{
+	if (!bt) return -1;
+	mgcu_lock();
+	double r = mgcu_batch_time_ms(bt->b, steps, flush_l2);
+	mgcu_unlock();
+	return r;
+}

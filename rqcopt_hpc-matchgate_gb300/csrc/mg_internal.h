@@ -101,6 +101,26 @@ int mgcu_plan_fetch(mgcu_plan* p, mgc* f, mgg* dblocks, mgc* hess);
 int mgcu_plan_project(mgcu_plan* p, const mgg* vblocks, double* grad_vec, double* H);
 long mgcu_plan_chunk_columns(const mgcu_plan* p);
 double mgcu_plan_time_ms(mgcu_plan* p, long b0, long b1, int steps, int flush_l2);
+
+/* ---- batches of instances (f and block gradients), persistent launches + CUDA graph ---- */
+typedef struct
+{
+	mgcu_target* target;   /* GPU circuit target on L qubits */
+	int L;
+	int ngates;            /* fitted circuit in sequential order */
+	const int* wires;      /* [2*ngates] */
+	int nblocks;
+	const int* block;      /* [ngates] */
+} mgcu_batch_inst;
+typedef struct mgcu_batch mgcu_batch;
+mgcu_batch* mgcu_batch_create(int n, const mgcu_batch_inst* insts, int precision, int tune);
+void mgcu_batch_destroy(mgcu_batch* b);
+int mgcu_batch_set_gates(mgcu_batch* b, int i, const mgg* gates);   /* [ngates_i] */
+int mgcu_batch_run(mgcu_batch* b);
+int mgcu_batch_fetch(mgcu_batch* b, int i, mgc* f, mgg* dblocks);
+int mgcu_batch_project(mgcu_batch* b, int i, const mgg* vblocks, double* grad_vec);
+int mgcu_batch_info(const mgcu_batch* b, int i, int* target_tile_bits, int* target_passes, int* items);
+double mgcu_batch_time_ms(mgcu_batch* b, int steps, int flush_l2);
 int mgcu_plan_target_kernel_ms(mgcu_plan* p, double* ms, long* launches);
 
 /* ---- FP64 algebra on the GPU ---- */

@@ -109,6 +109,15 @@ class MatchgateLib:
             L.mg_target_free.argtypes = [P]
             L.mg_target_set_resident.argtypes = [P, C.c_int]
             L.mg_target_sweep_gates.argtypes = [P]
+            L.mg_batch_create.restype = P
+            L.mg_batch_create.argtypes = [C.c_int, P, P, P, P, P, C.c_int]
+            L.mg_batch_set_gates.argtypes = [P, C.c_int, P]
+            L.mg_batch_run.argtypes = [P]
+            L.mg_batch_results.argtypes = [P, C.c_int, P, P, P]
+            L.mg_batch_info.argtypes = [P, C.c_int, P, P, P]
+            L.mg_batch_time_ms.argtypes = [P, C.c_int, C.c_int]
+            L.mg_batch_time_ms.restype = C.c_double
+            L.mg_batch_free.argtypes = [P]
             L.mg_last_error.restype = C.c_char_p
             L.mg_plan_brickwall.argtypes = [P, P, P, C.c_int, C.c_int, P, C.c_int]
             L.mg_plan_set_gates.argtypes = [P, P]
@@ -148,6 +157,57 @@ class MatchgateLib:
         if rc != 0:
             raise RuntimeError(self.last_error())
         return ms.value, n.value
+
+    # ------------------------------------------------------------------ batches
+    def batch_create(self, targets, vlists, perms_list, Ls, tune=True):
+        """mg_batch_create for n brickwall fits; returns an opaque batch (keeps its inputs alive)"""
+        n = len(targets)
+        keep = []
+        vl = [gates_arr(v) for v in vlists]
+        pps = []
+        for perms, L in zip(perms_list, Ls):
+            pp, rows = _perm_ptrs(perms, L)
+            keep.append((pp, rows))
+            pps.append(C.cast(pp, P).value)
+        T = (P * n)(*targets)
+        V = (P * n)(*[v.ctypes.data for v in vl])
+        NL = (C.c_int * n)(*[len(v) for v in vl])
+        PP = (P * n)(*pps)
+        LL = (C.c_int * n)(*[int(L) for L in Ls])
+        b = self.lib.mg_batch_create(n, T, V, NL, PP, LL, int(bool(tune)))
+        if not b:
+            raise RuntimeError(self.last_error())
+        return {"ptr": b, "n": n, "nlayers": [len(v) for v in vl], "keep": (keep, vl)}
+
+    def batch_set_gates(self, batch, i, vlist):
+        v = gates_arr(vlist)
+        return self.lib.mg_batch_set_gates(P(batch["ptr"]), i, _p(v))
+
+    def batch_run(self, batch):
+        return self.lib.mg_batch_run(P(batch["ptr"]))
+
+    def batch_results(self, batch, i):
+        """(f, dvlist [nlayers, 8], grad_vec [8 nlayers])"""
+        nl = batch["nlayers"][i]
+        f = np.zeros(1, cd); dv = np.zeros((nl, 8), cd); g = np.zeros(8 * nl)
+        rc = self.lib.mg_batch_results(P(batch["ptr"]), i, _p(f), _p(dv), _p(g))
+        if rc != 0:
+            raise RuntimeError(self.last_error())
+        return f[0], dv, g
+
+    def batch_info(self, batch, i):
+        kt, npass, items = C.c_int(), C.c_int(), C.c_int()
+        rc = self.lib.mg_batch_info(P(batch["ptr"]), i, C.byref(kt), C.byref(npass), C.byref(items))
+        if rc != 0:
+            raise RuntimeError(self.last_error())
+        return kt.value, npass.value, items.value
+
+    def batch_time_ms(self, batch, steps, flush_l2=True):
+        return self.lib.mg_batch_time_ms(P(batch["ptr"]), steps, int(bool(flush_l2)))
+
+    def batch_free(self, batch):
+        self.lib.mg_batch_free(P(batch["ptr"]))
+        batch["ptr"] = None
 
     def launch_count(self):
         return self.lib.mg_launch_count()
