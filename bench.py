@@ -47,9 +47,10 @@ def parse():
     ap.add_argument("--fp64-columns", type=int, default=2048, help="column sample for the FP64 comparison")
     ap.add_argument("--cpu-seconds", type=float, default=15.0, help="budget of the CPU baseline sample")
     ap.add_argument("--no-cpu", action="store_true")
-    ap.add_argument("--config", default="grad16", choices=["grad16", "grad18", "hess14"],
+    ap.add_argument("--config", default="grad16", choices=["grad16", "grad18", "hess14", "batch64"],
                     help="grad16: the headline (L=16 gradient, 5 layers); grad18: L=18 gradient, 7 layers, on a "
-                         "column sample; hess14: L=14 full Hessian, 9 layers")
+                         "column sample; hess14: L=14 full Hessian, 9 layers; batch64: 64 instances of uneven size "
+                         "in one batched launch sequence")
     ap.add_argument("--sample-columns", type=int, default=4096, help="column sample of --config grad18")
     ap.add_argument("--profile-columns", type=int, default=0,
                     help="small case for ncu: one evaluation over this many columns, no timing, then exit")
@@ -377,10 +378,85 @@ def run_secondary(a):
     print(json.dumps(out))
 
 
+def batch_workload(n=64, seed=4):
+    """64 instances: L ~ U{10,12,14,16}, fitted depth ~ U{3..9} (Haar-random layers),
+    target = a random matchgate brickwall of twice the depth; seeded"""
+    import numpy as np
+    import targets as T
+    rng = np.random.default_rng(seed)
+    out = []
+    for _ in range(n):
+        L = int(rng.choice([10, 12, 14, 16]))
+        nl = int(rng.integers(3, 10))
+        out.append({"L": L, "nl": nl, "ul": T.haar_matchgates(2 * nl, rng), "uperms": T.brickwall_perms(L, 2 * nl),
+                    "v": T.haar_matchgates(nl, rng), "perms": T.brickwall_perms(L, nl)})
+    return out
+
+
+def run_batch(a):
+    """config batch64: one batch of 64 uneven instances (f + gradient each) against the
+    same instances evaluated one plan at a time, mixed and FP64"""
+    import numpy as np
+    import mgcu
+    lib = mgcu.default_lib()
+    inst = batch_workload()
+    for x in inst:
+        x["t"] = lib.target_brickwall(x["ul"], x["uperms"], x["L"])
+    args = ([x["t"] for x in inst], [x["v"] for x in inst], [x["perms"] for x in inst], [x["L"] for x in inst])
+    out = {}
+    for name, prec in (("mixed", mgcu.PREC_MIXED), ("fp64", mgcu.PREC_FP64)):
+        lib.set_precision(prec)
+        b = lib.batch_create(*args)
+        n0 = lib.launch_count()
+        for _ in range(a.warmup if name == "mixed" else 1):
+            assert lib.batch_run(b) == 0, lib.last_error()
+        steps = a.steps if name == "mixed" else 1
+        n1 = lib.launch_count()
+        ms = lib.batch_time_ms(b, steps, True)
+        launches = (lib.launch_count() - n1) / steps
+        assert ms > 0, lib.last_error()
+        res = [lib.batch_results(b, i) for i in range(len(inst))]
+        info = [lib.batch_info(b, i) for i in range(len(inst))]
+        lib.batch_free(b)
+        out[name] = {"s_per_batch": ms / 1e3 / steps, "res": res, "info": info, "launches": launches}
+        if name == "mixed":
+            # the same instances one device-resident plan at a time
+            seq = 0.0
+            for x in inst:
+                plan = lib.plan_brickwall(lib.mg_target_apply, x["t"], x["v"], x["perms"], x["L"], mgcu.EVAL_GRADIENT)
+                assert lib.lib.mg_plan_run(mgcu.P(plan)) == 0
+                seq += lib.lib.mg_plan_time_ms(mgcu.P(plan), 1, 0)
+                lib.lib.mg_plan_free(mgcu.P(plan))
+            out["seq_mixed_s"] = seq / 1e3
+    for x in inst:
+        lib.target_free(x["t"])
+    ef = max(abs(m[0] - f[0]) / max(abs(f[0]), 1e-300) for m, f in zip(out["mixed"]["res"], out["fp64"]["res"]))
+    eg = max(float(np.linalg.norm(m[2] - f[2]) / max(np.linalg.norm(f[2]), 1e-300)) for m, f in zip(out["mixed"]["res"], out["fp64"]["res"]))
+    Ls = [x["L"] for x in inst]
+    tiles = {}
+    for x, (kt, npass, items) in zip(inst, out["mixed"]["info"]):
+        tiles.setdefault(x["L"], set()).add(kt)
+    print(json.dumps({
+        "metric": "batch evaluations/s (64 uneven instances, f + Riemannian gradient each)",
+        "value": 1.0 / out["mixed"]["s_per_batch"], "unit": "batches/s", "n_gpus": 1, "steps": a.steps, "warmup": a.warmup,
+        "ms_per_step": out["mixed"]["s_per_batch"] * 1e3, "higher_is_better": True, "dtype": "f32 float-float pairs, f64 sums",
+        "data": "synthetic (seed 4: L ~ U{10,12,14,16}, depth ~ U{3..9}, Haar layers; random brickwall targets of twice the depth)",
+        "config": {"workload": "64 instances in one batch: persistent batched launches per phase, captured CUDA graph",
+                   "instances_per_L": {str(L): Ls.count(L) for L in sorted(set(Ls))},
+                   "tuned_target_tile_bits_per_L": {str(L): sorted(v) for L, v in sorted(tiles.items())},
+                   "l2": "a 512 MiB buffer is written between timed replays"},
+        "gpu_launches": out["mixed"]["launches"],
+        "fp64_batch_s": out["fp64"]["s_per_batch"], "speedup_mixed_vs_fp64": out["fp64"]["s_per_batch"] / out["mixed"]["s_per_batch"],
+        "one_plan_at_a_time_mixed_s": out["seq_mixed_s"], "speedup_batch_vs_one_at_a_time": out["seq_mixed_s"] / out["mixed"]["s_per_batch"],
+        "accuracy": {"max_rel_err_f_vs_fp64": ef, "max_rel_err_grad_vs_fp64": eg}}))
+
+
 def main():
     a = parse()
     if a.impl == "reference":
         run_reference(a)
+    elif a.config == "batch64":
+        run_batch(a)
     elif a.config != "grad16":
         run_secondary(a)
     else:

@@ -88,6 +88,46 @@ double mg_batch_time_ms(mg_batch* batch, int steps, int flush_l2);
 void mg_batch_free(mg_batch* batch);
 
 /* ---------------------------------------------------------------------------------
+ * Request server (no reference counterpart): evaluations submitted from any thread and
+ * served by one worker thread with continuous batching.  Each step takes every queued
+ * request whose device workspace estimate fits what is left of the HBM budget (a later
+ * request may pass one that does not fit yet; one that can never fit fails with -6),
+ * runs all f / gradient requests of the step as one batch (as mg_batch_*), then the
+ * Hessian and trust-region-step requests on cached evaluation plans.  Requests that
+ * arrive during a step join the next one.  Precision: the library's current one.
+ * --------------------------------------------------------------------------------- */
+enum { MG_REQ_TARGET = 0, MG_REQ_GRADIENT = 1, MG_REQ_HESSIAN = 2, MG_REQ_TRSTEP = 3 };
+typedef struct
+{
+	int kind;                          /* MG_REQ_* */
+	void* target;                      /* GPU target (mg_target_*) on nqubits qubits */
+	int nqubits, nlayers;
+	const struct matchgate* vlist;     /* [nlayers], copied at submission */
+	const int* perms;                  /* [nlayers][nqubits] row-major, copied */
+	double radius;                     /* MG_REQ_TRSTEP: trust radius */
+} mg_request;
+typedef struct mg_server mg_server;
+mg_server* mg_server_create(size_t hbm_budget_bytes, int max_batch);
+/* returns the request id (>= 0) or an error code (< 0) */
+long mg_server_submit(mg_server* server, const mg_request* request);
+/* 1 when request id has completed, 0 while it is queued or running */
+int mg_server_done(mg_server* server, long id);
+/* block until request id completes; its status (0 or an error code) */
+int mg_server_wait(mg_server* server, long id);
+/* wait, then copy the results (any pointer may be NULL): f (Re f for a trust-region step,
+ * at the returned point), grad_vec [8 nlayers] and H [(8 nlayers)^2] (Riemannian, at the
+ * request's input point), vlist [nlayers] (a trust-region step's new point: the
+ * retracted step when accepted, else the input), the new radius and acceptance,
+ * times {submitted, started, completed} in seconds of CLOCK_MONOTONIC, and the step
+ * that served it */
+int mg_server_result(mg_server* server, long id, numeric* fval, double* grad_vec, double* H, struct matchgate vlist[],
+                     double* radius, int* accepted, double times[3], long* step);
+/* steps run, requests served in batches, largest budget in use by one step (bytes) */
+void mg_server_stats(mg_server* server, long* steps, long* batched, size_t* peak_bytes);
+/* serves what is queued, stops the worker and frees everything */
+void mg_server_free(mg_server* server);
+
+/* ---------------------------------------------------------------------------------
  * Results the reference computes only inside larger calls
  * --------------------------------------------------------------------------------- */
 

@@ -24,6 +24,7 @@ def _sources():
     cu = sorted(glob.glob(os.path.join(HERE, "csrc", "cuda", "*.cu")))
     c = sorted(glob.glob(os.path.join(HERE, "csrc", "host", "*.c")))
     hdr = (glob.glob(os.path.join(HERE, "csrc", "*.h")) + glob.glob(os.path.join(HERE, "csrc", "cuda", "*.cuh"))
+           + glob.glob(os.path.join(HERE, "csrc", "host", "*.h"))
            + glob.glob(os.path.join(ROOT, "include", "*.h")))
     return cu, c, hdr
 

@@ -866,7 +866,6 @@ struct BatchItem
 	int inst;      // instance
 	int slot;      // the item's partial row in its instance's part_f / part_g
 	long b0, b1;   // columns
-	long stage;    // element offset of column b0's target column in the staging buffer
 };
 
 __device__ __forceinline__ int next_item(int* counter, int* shared_slot)
@@ -878,21 +877,6 @@ __device__ __forceinline__ int next_item(int* counter, int* shared_slot)
 	return it;
 }
 
-template <class P>
-__global__ void __launch_bounds__(256, 2) k_target_batch(const Args<P>* __restrict__ args, const BatchItem* __restrict__ items,
-	int nitems, int* counter, typename P::T* stage)
-{
-	extern __shared__ __align__(16) char smem_raw[];
-	__shared__ int it_s;
-	for (;;)
-	{
-		const int it = next_item(counter, &it_s);
-		if (it >= nitems) break;
-		const BatchItem I = items[it];
-		const Args<P>& a = args[I.inst];
-		for (long b = I.b0; b < I.b1; b++) tgt_column<P>(a, b, stage + I.stage + (size_t)(b - I.b0) * a.S, smem_raw);
-	}
-}
 
 // ------------------------------------------------------------------------------------
 // stage A: per column -- W forward with cache, overlap, W backward; the target column
@@ -1025,16 +1009,33 @@ __global__ void __launch_bounds__(256) k_columns(Args<P> a)
 	block_reduce1<P>(facc, s.red, a.part_f + (size_t)blockIdx.x * 2);
 }
 
-// batched gradient items: target columns staged by k_target_batch; the block's slots and
-// gate cache live in per-block scratch (stride slot_stride / cache_stride elements)
+// out-of-line copies for the batched kernel, so that each phase gets its own register
+// allocation instead of one allocation spanning both
 template <class P>
-__global__ void __launch_bounds__(256) k_columns_batch(const Args<P>* __restrict__ args, const BatchItem* __restrict__ items,
-	int nitems, int* counter, const typename P::T* stage, typename P::T* scratch, long slot_stride, long cache_stride)
+__device__ __noinline__ void tgt_column_call(const Args<P>& a, long b, typename P::T* out, char* smem_raw)
+{
+	tgt_column<P>(a, b, out, smem_raw);
+}
+
+template <class P>
+__device__ __noinline__ void w_column_call(const Args<P>& a, long b, const typename P::T* dense, long prow,
+	typename P::T* su, typename P::T* sw, typename P::T* cache, typename P::Acc& facc, char* smem_raw)
+{
+	w_column<P, false>(a, b, dense, b, prow, su, sw, cache, nullptr, facc, smem_raw);
+}
+
+// batched items, target and fitted circuit per column: the target column goes into the
+// block's slot sx, then the fitted circuit runs against it; slots and gate cache live in
+// per-block scratch (3 slots of slot_stride, then cache_stride elements)
+template <class P>
+__global__ void __launch_bounds__(256, 2) k_batch(const Args<P>* __restrict__ args_t, const Args<P>* __restrict__ args_c,
+	const BatchItem* __restrict__ items, int nitems, int* counter, typename P::T* scratch, long slot_stride, long cache_stride)
 {
 	typedef typename P::T T;
 	extern __shared__ __align__(16) char smem_raw[];
 	__shared__ int it_s;
-	T* su = scratch + (size_t)blockIdx.x * (2 * slot_stride + cache_stride);
+	T* sx = scratch + (size_t)blockIdx.x * (3 * slot_stride + cache_stride);
+	T* su = sx + slot_stride;
 	T* sw = su + slot_stride;
 	T* cache = sw + slot_stride;
 	for (;;)
@@ -1042,10 +1043,14 @@ __global__ void __launch_bounds__(256) k_columns_batch(const Args<P>* __restrict
 		const int it = next_item(counter, &it_s);
 		if (it >= nitems) break;
 		const BatchItem I = items[it];
-		const Args<P>& a = args[I.inst];
+		const Args<P>& at = args_t[I.inst];
+		const Args<P>& a = args_c[I.inst];
 		typename P::Acc facc = P::acc_zero();
 		for (long b = I.b0; b < I.b1; b++)
-			w_column<P, false>(a, b, stage + I.stage, I.b0, I.slot, su, sw, a.want_grad ? cache : nullptr, nullptr, facc, smem_raw);
+		{
+			tgt_column_call<P>(at, b, sx, smem_raw);
+			w_column_call<P>(a, b, sx, I.slot, su, sw, a.want_grad ? cache : nullptr, facc, smem_raw);
+		}
 		T* tile;
 		Smem s = smem_layout<T>(smem_raw, a.kt, tile);
 		block_reduce1<P>(facc, s.red, a.part_f + (size_t)I.slot * 2);
@@ -1321,6 +1326,7 @@ struct mgcu_target
 	bool res_valid[3] = { false, false, false };
 	// the gate list the target sweep runs (fermionic swaps relabelled away, see
 	// relabel_fswaps) with per-gate Jordan-Wigner string wires
+	int tuned_kt[3][32] = {};      // batch tile choice per precision and L (0: not tuned yet)
 	bool sweep_ready = false;
 	std::vector<mgg> sg;
 	std::vector<int> sw;
@@ -2131,12 +2137,12 @@ struct mgcu_batch
 	int prec, n, threads = 256;
 	size_t tsize;
 	std::unique_ptr<BatchInst[]> inst;
-	DevBuf args_t, args_c, items, counters, stage, scratch, parts, red;
-	std::vector<int> round_beg;    // item index where each round starts (plus the end)
+	DevBuf args_t, args_c, items, counters, scratch, parts, red;
 	long slot_stride = 0, cache_stride = 0;
-	size_t smem_t = 0, smem_c = 0;
-	int grid_t = 0, grid_c = 0, nitems = 0;
+	size_t smem = 0;
+	int grid = 0, nitems = 0;
 	long graph_kernels = 0;        // kernel nodes per replay
+	bool use_graph = true;         // false: plain launches (a batch run once)
 	cudaGraph_t graph = nullptr;
 	cudaGraphExec_t exec = nullptr;
 	DevBuf flush;
@@ -2212,6 +2218,8 @@ static int batch_build(mgcu_batch* B, const mgcu_batch_inst* d, int tune)
 		I.kt_c = std::min(kt_default, I.nb);
 		const std::pair<mgcu_target*, int> key(D.target, D.L);
 		auto it = tuned.find(key);
+		if (it == tuned.end() && tune && D.target->tuned_kt[P::kId][D.L] > 0)
+			it = tuned.emplace(key, D.target->tuned_kt[P::kId][D.L]).first;
 		if (it == tuned.end())
 		{
 			int best_kt = std::min(kt_default, I.nb);
@@ -2226,6 +2234,7 @@ static int batch_build(mgcu_batch* B, const mgcu_batch_inst* d, int tune)
 				}
 			}
 			it = tuned.emplace(key, best_kt).first;
+			if (tune) D.target->tuned_kt[P::kId][D.L] = best_kt;
 		}
 		I.kt_t = it->second;
 		int e = build_target_prog<P>(D.target, I.kt_t, threads, I.tp);
@@ -2242,25 +2251,21 @@ static int batch_build(mgcu_batch* B, const mgcu_batch_inst* d, int tune)
 		if (e) return e;
 		MGCU_TRY(cudaMemcpy(I.d_block.p, D.block, sizeof(int) * D.ngates, cudaMemcpyHostToDevice));
 		I.col_cost = (double)I.S * ((double)mgcu_target_sweep_gates(D.target) + 3.0 * D.ngates);
-		B->smem_t = std::max(B->smem_t, I.smem_t);
-		B->smem_c = std::max(B->smem_c, I.smem_c);
+		B->smem = std::max(B->smem, std::max(I.smem_t, I.smem_c));
 		B->slot_stride = std::max(B->slot_stride, I.S);
-		B->cache_stride = std::max(B->cache_stride, I.S * D.ngates);
+		if (D.want_grad) B->cache_stride = std::max(B->cache_stride, I.S * D.ngates);
 	}
-	// the batched kernels also hold one static shared int: ask for exactly what they use
-	MGCU_TRY(cudaFuncSetAttribute(k_target_batch<P>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)B->smem_t));
-	MGCU_TRY(cudaFuncSetAttribute(k_columns_batch<P>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)B->smem_c));
-	int pt = 0, pc = 0;
-	MGCU_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&pt, k_target_batch<P>, threads, B->smem_t));
-	MGCU_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&pc, k_columns_batch<P>, threads, B->smem_c));
-	if (pt < 1 || pc < 1) { mg_set_error("batch: a block does not fit on an SM"); return MG_ERR_ARG; }
-	B->grid_t = c->nsm * pt;
-	B->grid_c = c->nsm * pc;
+	// the batched kernel also holds one static shared int: ask for exactly what it uses
+	MGCU_TRY(cudaFuncSetAttribute(k_batch<P>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)B->smem));
+	int pb = 0;
+	MGCU_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&pb, k_batch<P>, threads, B->smem));
+	if (pb < 1) { mg_set_error("batch: a block does not fit on an SM"); return MG_ERR_ARG; }
+	B->grid = c->nsm * pb;
 
 	// work items: about 16 per block, never more than an instance's columns, largest first
 	double total = 0;
 	for (int i = 0; i < B->n; i++) total += B->inst[i].col_cost * (double)(1L << B->inst[i].L);
-	const double item_cost = total / (16.0 * std::max(B->grid_t, B->grid_c));
+	const double item_cost = total / (16.0 * B->grid);
 	struct HostItem { BatchItem it; double cost; };
 	std::vector<HostItem> all;
 	for (int i = 0; i < B->n; i++)
@@ -2271,27 +2276,14 @@ static int batch_build(mgcu_batch* B, const mgcu_batch_inst* d, int tune)
 		for (long b0 = 0; b0 < N; b0 += per)
 		{
 			HostItem h;
-			h.it.inst = i; h.it.slot = I.nslots++; h.it.b0 = b0; h.it.b1 = std::min(N, b0 + per); h.it.stage = 0;
+			h.it.inst = i; h.it.slot = I.nslots++; h.it.b0 = b0; h.it.b1 = std::min(N, b0 + per);
 			h.cost = I.col_cost * (double)(h.it.b1 - h.it.b0);
 			all.push_back(h);
 		}
 	}
 	std::stable_sort(all.begin(), all.end(), [](const HostItem& x, const HostItem& y) { return x.cost > y.cost; });
-	// rounds: staged target columns of a round within 16 GB
-	const size_t budget = 16ull << 30;
 	std::vector<BatchItem> items;
-	size_t used = 0, max_used = 0;
-	B->round_beg.assign(1, 0);
-	for (HostItem& h : all)
-	{
-		const size_t bytes = sizeof(T) * (size_t)B->inst[h.it.inst].S * (size_t)(h.it.b1 - h.it.b0);
-		if (used + bytes > budget && used > 0) { B->round_beg.push_back((int)items.size()); used = 0; }
-		h.it.stage = (long)(used / sizeof(T));
-		used += bytes;
-		max_used = std::max(max_used, used);
-		items.push_back(h.it);
-	}
-	B->round_beg.push_back((int)items.size());
+	for (const HostItem& h : all) items.push_back(h.it);
 	B->nitems = (int)items.size();
 
 	// partial rows of every instance in one buffer
@@ -2302,12 +2294,10 @@ static int batch_build(mgcu_batch* B, const mgcu_batch_inst* d, int tune)
 		I.part_off = off; off += 2L * I.nslots;
 		I.part_g_off = off; off += 16L * I.nslots * std::max(I.ngates, 1);
 	}
-	const int nrounds = (int)B->round_beg.size() - 1;
 	int e = B->parts.alloc(sizeof(double) * std::max(off, 1L));
-	if (!e) e = B->stage.alloc(std::max<size_t>(max_used, 16));
-	if (!e) e = B->scratch.alloc(sizeof(T) * (size_t)B->grid_c * (size_t)(2 * B->slot_stride + B->cache_stride));
+	if (!e) e = B->scratch.alloc(sizeof(T) * (size_t)B->grid * (size_t)(3 * B->slot_stride + B->cache_stride));
 	if (!e) e = B->items.alloc(sizeof(BatchItem) * std::max<size_t>(items.size(), 1));
-	if (!e) e = B->counters.alloc(sizeof(int) * 2 * std::max(nrounds, 1));
+	if (!e) e = B->counters.alloc(sizeof(int) * 2);
 	if (!e) e = B->args_t.alloc(sizeof(Args<P>) * B->n);
 	if (!e) e = B->args_c.alloc(sizeof(Args<P>) * B->n);
 	if (!e) e = B->red.alloc(sizeof(BatchRed) * B->n);
@@ -2328,7 +2318,7 @@ static int batch_build(mgcu_batch* B, const mgcu_batch_inst* d, int tune)
 		memset(&w, 0, sizeof(w));
 		w.L = I.L; w.nb = I.nb; w.kt = I.kt_c; w.S = I.S;
 		w.W.pass = I.d_pass.as<PassRec>(); w.W.gate = I.d_gate.as<GateRec>(); w.W.npass = (int)I.ws.pass.size();
-		w.wm = I.d_mats.as<T>(); w.ngates = I.ngates; w.want_grad = 1;
+		w.wm = I.d_mats.as<T>(); w.ngates = I.ngates; w.want_grad = d[i].want_grad ? 1 : 0;
 		w.part_f = parts + I.part_off; w.part_g = parts + I.part_g_off;
 		BatchRed& r = rd[i];
 		r.part_f = parts + I.part_off; r.part_g = parts + I.part_g_off; r.block = I.d_block.as<int>();
@@ -2347,20 +2337,11 @@ static int batch_issue(mgcu_batch* B)
 {
 	typedef typename P::T T;
 	cudaStream_t st = mgcu_ctx()->stream;
-	const int nrounds = (int)B->round_beg.size() - 1;
 	MGCU_TRY(cudaMemsetAsync(B->parts.p, 0, B->parts.n, st));
 	MGCU_TRY(cudaMemsetAsync(B->counters.p, 0, B->counters.n, st));
-	for (int r = 0; r < nrounds; r++)
-	{
-		const int i0 = B->round_beg[r], ni = B->round_beg[r + 1] - i0;
-		const BatchItem* items = B->items.as<BatchItem>() + i0;
-		int* ctr = B->counters.as<int>() + 2 * r;
-		k_target_batch<P><<<std::min(B->grid_t, ni), B->threads, B->smem_t, st>>>(B->args_t.as<Args<P>>(), items, ni, ctr, B->stage.as<T>());
-		MGCU_LAUNCHED();
-		k_columns_batch<P><<<std::min(B->grid_c, ni), B->threads, B->smem_c, st>>>(B->args_c.as<Args<P>>(), items, ni, ctr + 1,
-			B->stage.as<T>(), B->scratch.as<T>(), B->slot_stride, B->cache_stride);
-		MGCU_LAUNCHED();
-	}
+	k_batch<P><<<std::min(B->grid, B->nitems), B->threads, B->smem, st>>>(B->args_t.as<Args<P>>(), B->args_c.as<Args<P>>(),
+		B->items.as<BatchItem>(), B->nitems, B->counters.as<int>(), B->scratch.as<T>(), B->slot_stride, B->cache_stride);
+	MGCU_LAUNCHED();
 	k_batch_reduce<<<B->n, 128, 0, st>>>(B->red.as<BatchRed>());
 	MGCU_LAUNCHED();
 	return 0;
@@ -2370,6 +2351,7 @@ template <class P>
 static int batch_issue_graph(mgcu_batch* B)
 {
 	cudaStream_t st = mgcu_ctx()->stream;
+	if (!B->use_graph) return batch_issue<P>(B);
 	if (!B->exec)
 	{
 		MGCU_TRY(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
@@ -2390,7 +2372,7 @@ static int batch_issue_graph(mgcu_batch* B)
 
 } // namespace
 
-extern "C" mgcu_batch* mgcu_batch_create(int n, const mgcu_batch_inst* d, int precision, int tune)
+extern "C" mgcu_batch* mgcu_batch_create(int n, const mgcu_batch_inst* d, int precision, int tune, int use_graph)
 {
 	if (!mgcu_ctx()) return nullptr;
 	if (n < 1) { mg_set_error("a batch needs at least one instance"); return nullptr; }
@@ -2401,7 +2383,7 @@ extern "C" mgcu_batch* mgcu_batch_create(int n, const mgcu_batch_inst* d, int pr
 			return nullptr;
 		}
 	mgcu_batch* B = new mgcu_batch();
-	B->prec = precision; B->n = n; B->tsize = prec_tsize(precision);
+	B->prec = precision; B->n = n; B->tsize = prec_tsize(precision); B->use_graph = use_graph != 0;
 	B->inst.reset(new BatchInst[n]);
 	int e;
 	if (precision == MG_PREC_FP64_ID) e = batch_build<PrecD>(B, d, tune);

@@ -13,18 +13,11 @@
 #include "matchgate_target.h"
 #include "mg_gb300.h"
 #include "../mg_internal.h"
+#include "mg_host.h"
 
 /* ======================================================================================
  * GPU target handles
  * ====================================================================================== */
-#define MG_TARGET_MAGIC 0x6d677467u
-
-typedef struct
-{
-	unsigned magic;
-	int L;
-	mgcu_target* dev;
-} mg_target_handle;
 
 static mg_target_handle* as_handle(linear_func f, void* udata)
 {
@@ -369,9 +362,7 @@ static int run_eval(linear_func ufunc, void* udata, const eval_req* q)
 }
 
 /* brickwall -> sequential circuit with one block per layer (src/matchgate_target.c:308-324) */
-typedef struct { struct matchgate* gates; int* wires; int* block; int ngates; } seq_circuit;
-
-static int brickwall_seq(const struct matchgate vlist[], int nlayers, int L, const int* perms[], seq_circuit* s)
+int brickwall_seq(const struct matchgate vlist[], int nlayers, int L, const int* perms[], seq_circuit* s)
 {
 	if (L % 2 || nlayers < 1)
 	{
@@ -396,7 +387,7 @@ static int brickwall_seq(const struct matchgate vlist[], int nlayers, int L, con
 	return 0;
 }
 
-static void seq_free(seq_circuit* s) { free(s->gates); free(s->wires); free(s->block); }
+void seq_free(seq_circuit* s) { free(s->gates); free(s->wires); free(s->block); }
 
 static int* identity_blocks(int n)
 {
@@ -680,10 +671,10 @@ mg_batch* mg_batch_create(int n, void* const targets[], const struct matchgate* 
 		if (!bt->vlist[i]) { free(d); mg_batch_free(bt); return NULL; }
 		memcpy(bt->vlist[i], vlists[i], sizeof(struct matchgate) * nlayers[i]);
 		d[i].target = th->dev; d[i].L = nqubits[i]; d[i].ngates = bt->s[i].ngates; d[i].wires = bt->s[i].wires;
-		d[i].nblocks = nlayers[i]; d[i].block = bt->s[i].block;
+		d[i].nblocks = nlayers[i]; d[i].block = bt->s[i].block; d[i].want_grad = 1;
 	}
 	mgcu_lock();
-	bt->b = mgcu_batch_create(n, d, mgcu_precision(), tune);
+	bt->b = mgcu_batch_create(n, d, mgcu_precision(), tune, 1);
 	int r = bt->b ? 0 : MG_ERR_DEVICE;
 	for (int i = 0; i < n && !r; i++) r = mgcu_batch_set_gates(bt->b, i, (const mgg*)bt->s[i].gates);
 	mgcu_unlock();

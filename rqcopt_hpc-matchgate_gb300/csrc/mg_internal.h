@@ -111,9 +111,10 @@ typedef struct
 	const int* wires;      /* [2*ngates] */
 	int nblocks;
 	const int* block;      /* [ngates] */
+	int want_grad;         /* 0: f only */
 } mgcu_batch_inst;
 typedef struct mgcu_batch mgcu_batch;
-mgcu_batch* mgcu_batch_create(int n, const mgcu_batch_inst* insts, int precision, int tune);
+mgcu_batch* mgcu_batch_create(int n, const mgcu_batch_inst* insts, int precision, int tune, int use_graph);
 void mgcu_batch_destroy(mgcu_batch* b);
 int mgcu_batch_set_gates(mgcu_batch* b, int i, const mgg* gates);   /* [ngates_i] */
 int mgcu_batch_run(mgcu_batch* b);

@@ -57,6 +57,15 @@ class RtrParams(C.Structure):
                 ("maxradius", C.c_double), ("g_func", C.c_void_p), ("g_data", C.c_void_p), ("g_iter", C.c_void_p)]
 
 
+class Request(C.Structure):
+    """mg_request of mg_gb300.h"""
+    _fields_ = [("kind", C.c_int), ("target", C.c_void_p), ("nqubits", C.c_int), ("nlayers", C.c_int),
+                ("vlist", C.c_void_p), ("perms", C.c_void_p), ("radius", C.c_double)]
+
+
+REQ_TARGET, REQ_GRADIENT, REQ_HESSIAN, REQ_TRSTEP = 0, 1, 2, 3
+
+
 def _p(a):
     return a.ctypes.data_as(P) if a is not None else None
 
@@ -118,6 +127,15 @@ class MatchgateLib:
             L.mg_batch_time_ms.argtypes = [P, C.c_int, C.c_int]
             L.mg_batch_time_ms.restype = C.c_double
             L.mg_batch_free.argtypes = [P]
+            L.mg_server_create.restype = P
+            L.mg_server_create.argtypes = [C.c_size_t, C.c_int]
+            L.mg_server_submit.restype = C.c_long
+            L.mg_server_submit.argtypes = [P, C.POINTER(Request)]
+            L.mg_server_done.argtypes = [P, C.c_long]
+            L.mg_server_wait.argtypes = [P, C.c_long]
+            L.mg_server_result.argtypes = [P, C.c_long, P, P, P, P, P, P, P, P]
+            L.mg_server_stats.argtypes = [P, P, P, P]
+            L.mg_server_free.argtypes = [P]
             L.mg_last_error.restype = C.c_char_p
             L.mg_plan_brickwall.argtypes = [P, P, P, C.c_int, C.c_int, P, C.c_int]
             L.mg_plan_set_gates.argtypes = [P, P]
@@ -208,6 +226,42 @@ class MatchgateLib:
     def batch_free(self, batch):
         self.lib.mg_batch_free(P(batch["ptr"]))
         batch["ptr"] = None
+
+    # ------------------------------------------------------------------ request server
+    def server_create(self, budget_bytes, max_batch=256):
+        s = self.lib.mg_server_create(int(budget_bytes), int(max_batch))
+        if not s:
+            raise RuntimeError(self.last_error())
+        return s
+
+    def server_submit(self, server, kind, target, vlist, perms, L, radius=0.0):
+        v = gates_arr(vlist)
+        pr = np.ascontiguousarray(np.asarray(perms, np.int32).reshape(len(v), L))
+        q = Request(kind, target, L, len(v), v.ctypes.data, pr.ctypes.data, radius)
+        rid = self.lib.mg_server_submit(P(server), C.byref(q))
+        if rid < 0:
+            raise RuntimeError(self.last_error())
+        return rid
+
+    def server_done(self, server, rid):
+        return self.lib.mg_server_done(P(server), rid) == 1
+
+    def server_result(self, server, rid, nlayers):
+        """dict: status, f, grad_vec, H, vlist, radius, accepted, times (submit, start, done), step"""
+        n = 8 * nlayers
+        f = np.zeros(1, cd); g = np.zeros(n); H = np.zeros((n, n)); v = np.zeros((nlayers, 8), cd)
+        rad = C.c_double(); acc = C.c_int(); t = np.zeros(3); step = C.c_long()
+        st = self.lib.mg_server_result(P(server), rid, _p(f), _p(g), _p(H), _p(v), C.byref(rad), C.byref(acc), _p(t), C.byref(step))
+        return {"status": st, "f": f[0], "grad_vec": g, "H": H, "vlist": v, "radius": rad.value, "accepted": bool(acc.value),
+                "times": t, "step": step.value}
+
+    def server_stats(self, server):
+        st, bt, pk = C.c_long(), C.c_long(), C.c_size_t()
+        self.lib.mg_server_stats(P(server), C.byref(st), C.byref(bt), C.byref(pk))
+        return st.value, bt.value, pk.value
+
+    def server_free(self, server):
+        self.lib.mg_server_free(P(server))
 
     def launch_count(self):
         return self.lib.mg_launch_count()
