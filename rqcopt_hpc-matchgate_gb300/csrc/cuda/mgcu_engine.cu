@@ -1009,21 +1009,6 @@ __global__ void __launch_bounds__(256) k_columns(Args<P> a)
 	block_reduce1<P>(facc, s.red, a.part_f + (size_t)blockIdx.x * 2);
 }
 
-// out-of-line copies for the batched kernel, so that each phase gets its own register
-// allocation instead of one allocation spanning both
-template <class P>
-__device__ __noinline__ void tgt_column_call(const Args<P>& a, long b, typename P::T* out, char* smem_raw)
-{
-	tgt_column<P>(a, b, out, smem_raw);
-}
-
-template <class P>
-__device__ __noinline__ void w_column_call(const Args<P>& a, long b, const typename P::T* dense, long prow,
-	typename P::T* su, typename P::T* sw, typename P::T* cache, typename P::Acc& facc, char* smem_raw)
-{
-	w_column<P, false>(a, b, dense, b, prow, su, sw, cache, nullptr, facc, smem_raw);
-}
-
 // batched items, target and fitted circuit per column: the target column goes into the
 // block's slot sx, then the fitted circuit runs against it; slots and gate cache live in
 // per-block scratch (3 slots of slot_stride, then cache_stride elements)
@@ -1048,8 +1033,8 @@ __global__ void __launch_bounds__(256, 2) k_batch(const Args<P>* __restrict__ ar
 		typename P::Acc facc = P::acc_zero();
 		for (long b = I.b0; b < I.b1; b++)
 		{
-			tgt_column_call<P>(at, b, sx, smem_raw);
-			w_column_call<P>(a, b, sx, I.slot, su, sw, a.want_grad ? cache : nullptr, facc, smem_raw);
+			tgt_column<P>(at, b, sx, smem_raw);
+			w_column<P, false>(a, b, sx, b, I.slot, su, sw, a.want_grad ? cache : nullptr, nullptr, facc, smem_raw);
 		}
 		T* tile;
 		Smem s = smem_layout<T>(smem_raw, a.kt, tile);
