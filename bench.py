@@ -47,10 +47,13 @@ def parse():
     ap.add_argument("--fp64-columns", type=int, default=2048, help="column sample for the FP64 comparison")
     ap.add_argument("--cpu-seconds", type=float, default=15.0, help="budget of the CPU baseline sample")
     ap.add_argument("--no-cpu", action="store_true")
-    ap.add_argument("--config", default="grad16", choices=["grad16", "grad18", "hess14", "batch64"],
+    ap.add_argument("--config", default="grad16", choices=["grad16", "grad18", "hess14", "batch64", "serve"],
                     help="grad16: the headline (L=16 gradient, 5 layers); grad18: L=18 gradient, 7 layers, on a "
                          "column sample; hess14: L=14 full Hessian, 9 layers; batch64: 64 instances of uneven size "
-                         "in one batched launch sequence")
+                         "in one batched launch sequence; serve: a seeded Poisson request stream through the "
+                         "request server")
+    ap.add_argument("--serve-requests", type=int, default=200)
+    ap.add_argument("--serve-max-L", type=int, default=16)
     ap.add_argument("--sample-columns", type=int, default=4096, help="column sample of --config grad18")
     ap.add_argument("--profile-columns", type=int, default=0,
                     help="small case for ncu: one evaluation over this many columns, no timing, then exit")
@@ -393,62 +396,142 @@ def batch_workload(n=64, seed=4):
     return out
 
 
+def _batch_eval(lib, mgcu, inst, prec, steps, warmup):
+    lib.set_precision(prec)
+    args = ([x["t"] for x in inst], [x["v"] for x in inst], [x["perms"] for x in inst], [x["L"] for x in inst])
+    b = lib.batch_create(*args)
+    for _ in range(warmup):
+        assert lib.batch_run(b) == 0, lib.last_error()
+    n1 = lib.launch_count()
+    ms = lib.batch_time_ms(b, steps, True)
+    assert ms > 0, lib.last_error()
+    launches = (lib.launch_count() - n1) / steps
+    res = [lib.batch_results(b, i) for i in range(len(inst))]
+    info = [lib.batch_info(b, i) for i in range(len(inst))]
+    lib.batch_free(b)
+    return {"s": ms / 1e3 / steps, "res": res, "info": info, "launches": launches}
+
+
+def _one_at_a_time(lib, mgcu, inst, prec):
+    lib.set_precision(prec)
+    tot = 0.0
+    for x in inst:
+        plan = lib.plan_brickwall(lib.mg_target_apply, x["t"], x["v"], x["perms"], x["L"], mgcu.EVAL_GRADIENT)
+        assert lib.lib.mg_plan_run(mgcu.P(plan)) == 0
+        tot += lib.lib.mg_plan_time_ms(mgcu.P(plan), 1, 0)
+        lib.lib.mg_plan_free(mgcu.P(plan))
+    return tot / 1e3
+
+
 def run_batch(a):
-    """config batch64: one batch of 64 uneven instances (f + gradient each) against the
-    same instances evaluated one plan at a time, mixed and FP64"""
+    """config batch64: one batch of 64 uneven instances (f + gradient each), against the
+    same instances one device-resident plan at a time; FP64 on the L<=14 instances"""
     import numpy as np
     import mgcu
     lib = mgcu.default_lib()
     inst = batch_workload()
     for x in inst:
         x["t"] = lib.target_brickwall(x["ul"], x["uperms"], x["L"])
-    args = ([x["t"] for x in inst], [x["v"] for x in inst], [x["perms"] for x in inst], [x["L"] for x in inst])
-    out = {}
-    for name, prec in (("mixed", mgcu.PREC_MIXED), ("fp64", mgcu.PREC_FP64)):
-        lib.set_precision(prec)
-        b = lib.batch_create(*args)
-        n0 = lib.launch_count()
-        for _ in range(a.warmup if name == "mixed" else 1):
-            assert lib.batch_run(b) == 0, lib.last_error()
-        steps = a.steps if name == "mixed" else 1
-        n1 = lib.launch_count()
-        ms = lib.batch_time_ms(b, steps, True)
-        launches = (lib.launch_count() - n1) / steps
-        assert ms > 0, lib.last_error()
-        res = [lib.batch_results(b, i) for i in range(len(inst))]
-        info = [lib.batch_info(b, i) for i in range(len(inst))]
-        lib.batch_free(b)
-        out[name] = {"s_per_batch": ms / 1e3 / steps, "res": res, "info": info, "launches": launches}
-        if name == "mixed":
-            # the same instances one device-resident plan at a time
-            seq = 0.0
-            for x in inst:
-                plan = lib.plan_brickwall(lib.mg_target_apply, x["t"], x["v"], x["perms"], x["L"], mgcu.EVAL_GRADIENT)
-                assert lib.lib.mg_plan_run(mgcu.P(plan)) == 0
-                seq += lib.lib.mg_plan_time_ms(mgcu.P(plan), 1, 0)
-                lib.lib.mg_plan_free(mgcu.P(plan))
-            out["seq_mixed_s"] = seq / 1e3
+    mx = _batch_eval(lib, mgcu, inst, mgcu.PREC_MIXED, a.steps, a.warmup)
+    seq = _one_at_a_time(lib, mgcu, inst, mgcu.PREC_MIXED)
+    small = [x for x in inst if x["L"] <= 12]
+    mx_small = _batch_eval(lib, mgcu, small, mgcu.PREC_MIXED, 3, 1)
+    seq_small = _one_at_a_time(lib, mgcu, small, mgcu.PREC_MIXED)
+    sub = [i for i, x in enumerate(inst) if x["L"] <= 14]
+    fp = _batch_eval(lib, mgcu, [inst[i] for i in sub], mgcu.PREC_FP64, 1, 1)
+    mx_sub = _batch_eval(lib, mgcu, [inst[i] for i in sub], mgcu.PREC_MIXED, 1, 1)
+    lib.set_precision(mgcu.PREC_MIXED)
     for x in inst:
         lib.target_free(x["t"])
-    ef = max(abs(m[0] - f[0]) / max(abs(f[0]), 1e-300) for m, f in zip(out["mixed"]["res"], out["fp64"]["res"]))
-    eg = max(float(np.linalg.norm(m[2] - f[2]) / max(np.linalg.norm(f[2]), 1e-300)) for m, f in zip(out["mixed"]["res"], out["fp64"]["res"]))
+    ef = max(abs(mx["res"][i][0] - f[0]) / max(abs(f[0]), 1e-300) for i, f in zip(sub, fp["res"]))
+    eg = max(float(np.linalg.norm(mx["res"][i][2] - f[2]) / max(np.linalg.norm(f[2]), 1e-300)) for i, f in zip(sub, fp["res"]))
     Ls = [x["L"] for x in inst]
     tiles = {}
-    for x, (kt, npass, items) in zip(inst, out["mixed"]["info"]):
+    for x, (kt, npass, items) in zip(inst, mx["info"]):
         tiles.setdefault(x["L"], set()).add(kt)
     print(json.dumps({
         "metric": "batch evaluations/s (64 uneven instances, f + Riemannian gradient each)",
-        "value": 1.0 / out["mixed"]["s_per_batch"], "unit": "batches/s", "n_gpus": 1, "steps": a.steps, "warmup": a.warmup,
-        "ms_per_step": out["mixed"]["s_per_batch"] * 1e3, "higher_is_better": True, "dtype": "f32 float-float pairs, f64 sums",
+        "value": 1.0 / mx["s"], "unit": "batches/s", "n_gpus": 1, "steps": a.steps, "warmup": a.warmup,
+        "ms_per_step": mx["s"] * 1e3, "higher_is_better": True, "dtype": "f32 float-float pairs, f64 sums",
         "data": "synthetic (seed 4: L ~ U{10,12,14,16}, depth ~ U{3..9}, Haar layers; random brickwall targets of twice the depth)",
-        "config": {"workload": "64 instances in one batch: persistent batched launches per phase, captured CUDA graph",
+        "config": {"workload": "64 instances in one batch: one persistent fused launch (target sweep + fitted circuit per "
+                               "column, work items largest first), captured CUDA graph",
                    "instances_per_L": {str(L): Ls.count(L) for L in sorted(set(Ls))},
                    "tuned_target_tile_bits_per_L": {str(L): sorted(v) for L, v in sorted(tiles.items())},
                    "l2": "a 512 MiB buffer is written between timed replays"},
-        "gpu_launches": out["mixed"]["launches"],
-        "fp64_batch_s": out["fp64"]["s_per_batch"], "speedup_mixed_vs_fp64": out["fp64"]["s_per_batch"] / out["mixed"]["s_per_batch"],
-        "one_plan_at_a_time_mixed_s": out["seq_mixed_s"], "speedup_batch_vs_one_at_a_time": out["seq_mixed_s"] / out["mixed"]["s_per_batch"],
-        "accuracy": {"max_rel_err_f_vs_fp64": ef, "max_rel_err_grad_vs_fp64": eg}}))
+        "gpu_launches": mx["launches"],
+        "one_plan_at_a_time_s": seq, "speedup_batch_vs_one_at_a_time": seq / mx["s"],
+        "small_instances": {"instances": len(small), "L": "10, 12", "batch_s": mx_small["s"], "one_plan_at_a_time_s": seq_small,
+                            "speedup": seq_small / mx_small["s"]},
+        "fp64_subset": {"instances": len(sub), "L": "<= 14", "fp64_batch_s": fp["s"], "mixed_batch_s": mx_sub["s"],
+                        "speedup_mixed_vs_fp64": fp["s"] / mx_sub["s"]},
+        "accuracy": {"max_rel_err_f_vs_fp64": ef, "max_rel_err_grad_vs_fp64": eg, "instances": len(sub)}}))
+
+
+def run_serve(a):
+    """config serve: a seeded Poisson stream (200 requests/s) of f / gradient / Hessian /
+    trust-region-step requests (40/40/10/10 %) through the request server, mixed
+    precision, HBM budget 120 GB; latency = completion - submission per request"""
+    import threading
+    import numpy as np
+    import mgcu
+    import targets as T
+    lib = mgcu.default_lib()
+    lib.set_precision(mgcu.PREC_MIXED)
+    rng = np.random.default_rng(5)
+    n = a.serve_requests
+    arrivals = np.cumsum(rng.exponential(1 / 200.0, size=n))
+    kinds = rng.choice([mgcu.REQ_TARGET, mgcu.REQ_GRADIENT, mgcu.REQ_HESSIAN, mgcu.REQ_TRSTEP], size=n, p=[0.4, 0.4, 0.1, 0.1])
+    Lmax = a.serve_max_L
+    reqs = []
+    for k in kinds:
+        # Hessians and trust-region steps (G^2 work per column) on L <= 12
+        L = int(rng.choice([x for x in range(10, (Lmax if k <= mgcu.REQ_GRADIENT else 12) + 1, 2)]))
+        nl = int(rng.integers(3, 10))
+        ul = T.haar_matchgates(2 * nl, rng)
+        reqs.append({"kind": int(k), "L": L, "nl": nl, "t": lib.target_brickwall(ul, T.brickwall_perms(L, 2 * nl), L),
+                     "v": T.near_identity_brickwall(nl, rng), "perms": T.brickwall_perms(L, nl)})
+    sv = lib.server_create(120 << 30)
+    # warm-up outside the measured stream: module loading and the first plans
+    for x in reqs[:10]:
+        lib.server_result(sv, lib.server_submit(sv, x["kind"], x["t"], x["v"], x["perms"], x["L"], 0.05), x["nl"])
+    steps0, batched0, _ = lib.server_stats(sv)
+    ids = [None] * n
+    t0 = time.perf_counter()
+
+    def producer():
+        for i, x in enumerate(reqs):
+            dt = t0 + arrivals[i] - time.perf_counter()
+            if dt > 0:
+                time.sleep(dt)
+            ids[i] = lib.server_submit(sv, x["kind"], x["t"], x["v"], x["perms"], x["L"], 0.05)
+    th = threading.Thread(target=producer)
+    th.start()
+    th.join()
+    res = [lib.server_result(sv, ids[i], x["nl"]) for i, x in enumerate(reqs)]
+    steps1, batched1, peak = lib.server_stats(sv)
+    lib.server_free(sv)
+    for x in reqs:
+        lib.target_free(x["t"])
+    assert all(r["status"] == 0 for r in res)
+    lat = np.array([(r["times"][2] - r["times"][0]) * 1e3 for r in res])
+    span = max(r["times"][2] for r in res) - min(r["times"][0] for r in res)
+    by_kind = {}
+    for name, k in (("target", 0), ("gradient", 1), ("hessian", 2), ("trstep", 3)):
+        l = lat[[i for i, x in enumerate(reqs) if x["kind"] == k]]
+        if len(l):
+            by_kind[name] = {"n": int(len(l)), "p50_ms": float(np.percentile(l, 50)), "p99_ms": float(np.percentile(l, 99))}
+    print(json.dumps({
+        "metric": "serving p50/p99 latency (ms) and throughput (requests/s)", "value": float(np.percentile(lat, 50)),
+        "unit": "ms (p50)", "p99_ms": float(np.percentile(lat, 99)), "throughput_rps": n / span, "n_gpus": 1,
+        "higher_is_better": False, "dtype": "f32 float-float pairs, f64 sums",
+        "data": f"synthetic (seed 5): {n} requests, Poisson arrivals at 200/s, mix 40/40/10/10 target/gradient/Hessian/TR step, "
+                f"depth U{{3..9}}, random brickwall targets of twice the depth; L U{{10..{Lmax}}} even (Hessian and TR step: "
+                "L U{10, 12})",
+        "config": {"workload": "request server, continuous batching, HBM budget 120 GB", "steps": steps1 - steps0,
+                   "requests_batched": batched1 - batched0, "peak_step_budget_bytes": peak,
+                   "offered_rate_rps": 200.0, "stream_s": float(arrivals[-1])},
+        "by_kind": by_kind}))
 
 
 def main():
@@ -457,6 +540,8 @@ def main():
         run_reference(a)
     elif a.config == "batch64":
         run_batch(a)
+    elif a.config == "serve":
+        run_serve(a)
     elif a.config != "grad16":
         run_secondary(a)
     else:

@@ -3,12 +3,14 @@
  * for brickwall fits against GPU targets, submitted from any thread and served by one
  * worker thread that owns the GPU.
  *
- * Continuous batching: the worker takes every queued request whose workspace estimate
- * fits the HBM budget left in the current step (requests arriving later may pass a
- * request that does not fit yet), runs all f / gradient requests of the step together in
- * one batch (persistent launches over all their columns), then the Hessian and
- * trust-region requests on device-resident evaluation plans (cached per shape), and
- * completes them; requests that arrive meanwhile wait for the next step.  Targets stay
+ * Continuous batching: each step the worker takes queued requests, shortest estimated
+ * work first (a request queued longer than the aging limit goes first), while their
+ * workspace estimates fit the HBM budget and their summed work stays within a step
+ * quantum (at least one request per step), so small requests are not held behind large
+ * ones.  It runs all f / gradient requests of the step together in one batch (one
+ * persistent launch over all their columns), then the Hessian and trust-region requests
+ * on device-resident evaluation plans (cached per shape), and completes them; requests
+ * that arrive meanwhile wait for the next step.  Targets stay
  * resident (they are the caller's GPU target handles).  The reference has no server;
  * the arithmetic of every request is the library's ordinary evaluation, so a result is
  * the same alone and in a mix up to summation order.
@@ -39,6 +41,7 @@ typedef struct
 	double* H;                   /* [(8 nlayers)^2] (HESSIAN, TRSTEP) */
 	double t_submit, t_start, t_done;
 	size_t est;
+	double work;                 /* estimated work, in amplitude-gate updates */
 	long step;
 } req_t;
 
@@ -74,6 +77,24 @@ static size_t estimate(const req_t* r)
 	const size_t hc = 2 * N * G * S * ts;
 	return (hc < cap16 ? hc : cap16) + (cols < cap8 ? cols : cap8) + 4 * blocks * S * ts;
 }
+
+/* amplitude-gate updates: target and fitted sweeps per column (backward counted three
+ * times), Hessian items pushing states through the later gates */
+static double work_of(const req_t* r)
+{
+	const double S = (double)((size_t)1 << (r->L - 1)), N = (double)((size_t)1 << r->L), G = (double)r->nlayers * (r->L / 2);
+	mgcu_lock();
+	const double gu = mgcu_target_sweep_gates(((const mg_target_handle*)r->target)->dev);
+	mgcu_unlock();
+	double w = N * S * (gu + (r->kind == MG_REQ_TARGET ? 1.0 : 3.0) * G);
+	if (r->kind >= MG_REQ_HESSIAN) w += N * S * 8.0 * G * G / 2.0 * (r->kind == MG_REQ_TRSTEP ? 1.1 : 1.0);
+	return w;
+}
+
+/* work one step may take: about a quarter second of the target sweep at L=16 */
+#define STEP_QUANTUM 2.0e11
+/* a request queued this long (s) is taken first */
+#define AGING_S 2.0
 
 static const int** perm_rows(const req_t* r, const int** rows)
 {
@@ -165,7 +186,8 @@ static void run_batch(req_t** rs, int n)
 	if (!rc)
 	{
 		mgcu_lock();
-		b = mgcu_batch_create(n, d, mgcu_precision(), 1, 0);
+		/* a step's batch runs once: no tile timing, no graph */
+		b = mgcu_batch_create(n, d, mgcu_precision(), 0, 0);
 		rc = b ? 0 : MG_ERR_DEVICE;
 		for (int i = 0; i < n && !rc; i++) rc = mgcu_batch_set_gates(b, i, (const mgg*)s[i].gates);
 		if (!rc) rc = mgcu_batch_run(b);
@@ -196,20 +218,33 @@ static void* worker(void* arg)
 		for (;;)
 		{
 			size_t used = 0;
+			double work = 0;
 			n = 0;
-			for (long id = sv->next_queued; id < sv->nreq && n < sv->max_batch; id++)
+			const double tnow = now_s();
+			for (;;)
 			{
-				req_t* r = sv->reqs[id];
-				if (r->state != ST_QUEUED) continue;
-				if (r->est > sv->budget)
+				/* next: the oldest request past the aging limit, else the least work */
+				req_t* best = NULL;
+				for (long id = sv->next_queued; id < sv->nreq; id++)
 				{
-					/* can never fit: fail it */
-					r->status = MG_ERR_ARG; r->state = ST_DONE; r->t_start = r->t_done = now_s();
-					continue;
+					req_t* r = sv->reqs[id];
+					if (r->state != ST_QUEUED) continue;
+					if (r->est > sv->budget)
+					{
+						/* can never fit: fail it */
+						r->status = MG_ERR_ARG; r->state = ST_DONE; r->t_start = r->t_done = now_s();
+						continue;
+					}
+					if (r->work < 0) r->work = work_of(r);
+					if (used + r->est > sv->budget || (n > 0 && work + r->work > STEP_QUANTUM)) continue;
+					const int aged = tnow - r->t_submit > AGING_S, best_aged = best && tnow - best->t_submit > AGING_S;
+					if (!best || (aged && !best_aged) || (aged == best_aged && !aged && r->work < best->work)) best = r;
 				}
-				if (used + r->est > sv->budget) continue;
-				used += r->est;
-				step[n++] = r;
+				if (!best || n >= sv->max_batch) break;
+				best->state = ST_RUNNING;
+				used += best->est;
+				work += best->work;
+				step[n++] = best;
 			}
 			while (sv->next_queued < sv->nreq && sv->reqs[sv->next_queued]->state != ST_QUEUED) sv->next_queued++;
 			if (n > 0 || sv->stop) { if (used > sv->peak) sv->peak = used; break; }
@@ -297,6 +332,7 @@ long mg_server_submit(mg_server* sv, const mg_request* q)
 	memcpy(r->vlist, q->vlist, sizeof(struct matchgate) * q->nlayers);
 	memcpy(r->perms, q->perms, sizeof(int) * (size_t)q->nlayers * q->nqubits);
 	r->est = estimate(r);
+	r->work = -1;   /* computed by the worker (it may need the library lock) */
 	pthread_mutex_lock(&sv->mu);
 	if (sv->nreq == sv->cap)
 	{
