@@ -781,8 +781,9 @@ __device__ __forceinline__ void tgt_gates(char* tb, const TGate* gates, int gbeg
 	}
 }
 
-// -conj(U e_b) of one basis column b into out (the whole block)
-template <class P>
+// -conj(U e_b) of one basis column b into out (the whole block); QPT: quartets per
+// thread and gate (0: any, one quartet per iteration)
+template <class P, int QPT>
 __device__ __forceinline__ void tgt_column(const Args<P>& a, long b, typename P::T* out, char* smem_raw)
 {
 	typedef typename P::T T;
@@ -793,7 +794,6 @@ __device__ __forceinline__ void tgt_column(const Args<P>& a, long b, typename P:
 	T* pm = reinterpret_cast<T*>(smem_raw + a.pm_off);   // this pass's distinct matrices
 	const int kt = a.kt;
 	const unsigned n = 1u << kt, Q = n >> 2;
-	const int qpt = (Q == 4u * blockDim.x) ? 4 : (Q == 8u * blockDim.x) ? 8 : 0;
 	{
 		const int par = __popcll(b) & 1;
 		const unsigned cb = (unsigned)(b >> 1);
@@ -834,9 +834,7 @@ __device__ __forceinline__ void tgt_column(const Args<P>& a, long b, typename P:
 						}
 					}
 				__syncthreads();
-				if (qpt == 4) tgt_gates<P, 4>(tb, a.utg, pr.gbeg, pr.gend, pm, tpar, nlb, Q);
-				else if (qpt == 8) tgt_gates<P, 8>(tb, a.utg, pr.gbeg, pr.gend, pm, tpar, nlb, Q);
-				else tgt_gates<P, 0>(tb, a.utg, pr.gbeg, pr.gend, pm, tpar, nlb, Q);
+				tgt_gates<P, QPT>(tb, a.utg, pr.gbeg, pr.gend, pm, tpar, nlb, Q);
 				for (unsigned e = threadIdx.x; e < n; e += blockDim.x)
 				{
 					const T v = tile[tsw<ES>(e)];
@@ -848,12 +846,35 @@ __device__ __forceinline__ void tgt_column(const Args<P>& a, long b, typename P:
 	}
 }
 
-template <class P, int NT>
-__global__ void __launch_bounds__(NT, 512 / NT) k_target(Args<P> a)
+// one instantiation per (block size, quartets per thread), so that each keeps only its
+// own path's registers: 256 threads with 4, 8 or any quartets; 512 with 2, 4 or any
+template <class P, int NT, int QPT>
+__global__ void __launch_bounds__(NT, (NT == 512 && QPT == 4) ? 1 : 2) k_target(Args<P> a)
 {
 	extern __shared__ __align__(16) char smem_raw[];
 	for (long b = a.b0 + blockIdx.x; b < a.b1; b += gridDim.x)
-		tgt_column<P>(a, b, a.ucols + (size_t)(b - a.b0) * a.S, smem_raw);
+		tgt_column<P, QPT>(a, b, a.ucols + (size_t)(b - a.b0) * a.S, smem_raw);
+}
+
+// the k_target instantiation for a tile of 2^kt amplitudes and a block size
+template <class P>
+static void (*target_kernel(int kt, int threads))(Args<P>)
+{
+	const long q = (1L << (kt - 2)) / threads, exact = (1L << (kt - 2)) % threads == 0;
+	if (threads > 256) return (exact && q == 2) ? k_target<P, 512, 2> : (exact && q == 4) ? k_target<P, 512, 4> : k_target<P, 512, 0>;
+	if (exact && q == 4) return k_target<P, 256, 4>;
+	if (exact && q == 8) return k_target<P, 256, 8>;
+	return k_target<P, 256, 0>;
+}
+
+// the same dispatch inside a kernel (batches: each item has its own tile size)
+template <class P>
+__device__ __forceinline__ void tgt_column_rt(const Args<P>& a, long b, typename P::T* out, char* smem_raw)
+{
+	const unsigned Q = 1u << (a.kt - 2);
+	if (Q == 4u * blockDim.x) tgt_column<P, 4>(a, b, out, smem_raw);
+	else if (Q == 8u * blockDim.x) tgt_column<P, 8>(a, b, out, smem_raw);
+	else tgt_column<P, 0>(a, b, out, smem_raw);
 }
 
 // ------------------------------------------------------------------------------------
@@ -1033,7 +1054,7 @@ __global__ void __launch_bounds__(256, 2) k_batch(const Args<P>* __restrict__ ar
 		typename P::Acc facc = P::acc_zero();
 		for (long b = I.b0; b < I.b1; b++)
 		{
-			tgt_column<P>(at, b, sx, smem_raw);
+			tgt_column_rt<P>(at, b, sx, smem_raw);
 			w_column<P, false>(a, b, sx, b, I.slot, su, sw, a.want_grad ? cache : nullptr, nullptr, facc, smem_raw);
 		}
 		T* tile;
@@ -1696,8 +1717,9 @@ static int launch_target(mgcu_plan* p, long b0, long b1, typename P::T* out)
 			p->kev.push_back(ev);
 		}
 	if (p->ktime) MGCU_TRY(cudaEventRecord(p->kev[p->kev_used], c->stream));
-	if (p->threads_t > 256) k_target<P, 512><<<grid, p->threads_t, p->smem_t, c->stream>>>(a);
-	else k_target<P, 256><<<grid, p->threads_t, p->smem_t, c->stream>>>(a);
+	void (*kern)(Args<P>) = target_kernel<P>(p->kt_t, p->threads_t);
+	if (!kern) { mg_set_error("no target-sweep kernel for 2^%d amplitudes and %d threads", p->kt_t, p->threads_t); return MG_ERR_ARG; }
+	kern<<<grid, p->threads_t, p->smem_t, c->stream>>>(a);
 	MGCU_LAUNCHED();
 	if (p->ktime) { MGCU_TRY(cudaEventRecord(p->kev[p->kev_used + 1], c->stream)); p->kev_used += 2; }
 	return 0;
@@ -1747,20 +1769,22 @@ static int set_smem_attr()
 {
 	MgcuContext* c = mgcu_ctx();
 	MGCU_TRY(cudaFuncSetAttribute(k_columns<P, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)std::min<size_t>(c->smem_optin, 227 * 1024)));
-	MGCU_TRY(cudaFuncSetAttribute(k_target<P, 256>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)std::min<size_t>(c->smem_optin, 227 * 1024)));
-	MGCU_TRY(cudaFuncSetAttribute(k_target<P, 512>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)std::min<size_t>(c->smem_optin, 227 * 1024)));
+	void (*const tk[6])(Args<P>) = { k_target<P, 256, 4>, k_target<P, 256, 8>, k_target<P, 256, 0>, k_target<P, 512, 2>,
+		k_target<P, 512, 4>, k_target<P, 512, 0> };
+	for (auto k : tk) MGCU_TRY(cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)std::min<size_t>(c->smem_optin, 227 * 1024)));
 	MGCU_TRY(cudaFuncSetAttribute(k_hessian<P>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)std::min<size_t>(c->smem_optin, 227 * 1024)));
 	return 0;
 }
 
 template <class P>
-static int occupancy(int threads, size_t smem, int threads_t, size_t smem_t, int& per_sm, int& per_sm_target)
+static int occupancy(int threads, size_t smem, int kt_t, int threads_t, size_t smem_t, int& per_sm, int& per_sm_target)
 {
 	int n1 = 0, n2 = 0, n3 = 0;
 	MGCU_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n1, k_columns<P, false>, threads, smem));
 	MGCU_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n2, k_hessian<P>, threads, smem));
-	if (threads_t > 256) MGCU_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n3, k_target<P, 512>, threads_t, smem_t));
-	else MGCU_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n3, k_target<P, 256>, threads_t, smem_t));
+	void (*kern)(Args<P>) = target_kernel<P>(kt_t, threads_t);
+	if (!kern) { mg_set_error("no target-sweep kernel for 2^%d amplitudes and %d threads", kt_t, threads_t); return MG_ERR_ARG; }
+	MGCU_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n3, kern, threads_t, smem_t));
 	per_sm = std::max(1, std::min(n1, n2));
 	per_sm_target = std::max(1, n3);
 	return 0;
@@ -1829,9 +1853,9 @@ extern "C" mgcu_plan* mgcu_plan_create(const mgcu_plan_desc* d)
 			+ std::max<size_t>((size_t)(tt / 32) * 16 * sizeof(double), 16 * 16) + (size_t)MAXPM * 8 * p->tsize;
 	}
 	int per_sm = 1, per_sm_t = 1, e = 0;
-	if (p->prec == MG_PREC_FP64_ID) { e = set_smem_attr<PrecD>(); if (!e) e = occupancy<PrecD>(threads, p->smem, p->threads_t, p->smem_t, per_sm, per_sm_t); }
-	else if (p->prec == MG_PREC_FP32_ID) { e = set_smem_attr<PrecF>(); if (!e) e = occupancy<PrecF>(threads, p->smem, p->threads_t, p->smem_t, per_sm, per_sm_t); }
-	else { e = set_smem_attr<PrecX>(); if (!e) e = occupancy<PrecX>(threads, p->smem, p->threads_t, p->smem_t, per_sm, per_sm_t); }
+	if (p->prec == MG_PREC_FP64_ID) { e = set_smem_attr<PrecD>(); if (!e) e = occupancy<PrecD>(threads, p->smem, p->kt_t, p->threads_t, p->smem_t, per_sm, per_sm_t); }
+	else if (p->prec == MG_PREC_FP32_ID) { e = set_smem_attr<PrecF>(); if (!e) e = occupancy<PrecF>(threads, p->smem, p->kt_t, p->threads_t, p->smem_t, per_sm, per_sm_t); }
+	else { e = set_smem_attr<PrecX>(); if (!e) e = occupancy<PrecX>(threads, p->smem, p->kt_t, p->threads_t, p->smem_t, per_sm, per_sm_t); }
 	if (e) { delete p; return nullptr; }
 	const long opt_cps = mgcu_option(MG_OPT_CTAS_PER_SM_ID);
 	if (opt_cps > 0) per_sm = (int)std::min<long>(per_sm, opt_cps);
@@ -2168,13 +2192,14 @@ static double time_target(mgcu_target* t, int L, int kt, int threads, long ncols
 	a.utg = tp.tg.as<TGate>(); a.upm = tp.pm.as<int2>(); a.upmats = tp.pmats.as<T>(); a.pm_off = (unsigned)pm_off;
 	a.b0 = 0; a.b1 = ncols; a.ucols = out.as<T>();
 	int per_sm = 0;
-	if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_target<P, 256>, threads, smem) != cudaSuccess || per_sm < 1) return -1;
+	void (*kern)(Args<P>) = target_kernel<P>(kt, threads);
+	if (!kern || cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, threads, smem) != cudaSuccess || per_sm < 1) return -1;
 	const int grid = (int)std::min<long>(std::min<long>((long)c->nsm * per_sm, grid_cap), ncols);
 	double best = -1;
 	for (int rep = 0; rep < 2; rep++)
 	{
 		cudaEventRecord(c->ev0, c->stream);
-		k_target<P, 256><<<grid, threads, smem, c->stream>>>(a);
+		kern<<<grid, threads, smem, c->stream>>>(a);
 		cudaEventRecord(c->ev1, c->stream);
 		if (cudaEventSynchronize(c->ev1) != cudaSuccess) return -1;
 		float ms = 0;
@@ -2190,7 +2215,10 @@ static int batch_build(mgcu_batch* B, const mgcu_batch_inst* d, int tune)
 	typedef typename P::T T;
 	MgcuContext* c = mgcu_ctx();
 	const int threads = B->threads;
-	MGCU_TRY(cudaFuncSetAttribute(k_target<P, 256>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)std::min<size_t>(c->smem_optin, 227 * 1024)));
+	{
+		const int e = set_smem_attr<P>();
+		if (e) return e;
+	}
 	const int kt_default = sizeof(T) >= 16 ? 12 : 13;
 	// tile choice per distinct (target, L): time the candidates on a column sample
 	std::map<std::pair<mgcu_target*, int>, int> tuned;

@@ -418,7 +418,8 @@ def test_hubbard_target_vs_oracle(lib, oracle):
                                                       (12, 9, 0, mgcu.PREC_FP64), (14, 12, 0, mgcu.PREC_MIXED),
                                                       (14, 12, 128, mgcu.PREC_FP64), (14, 10, 0, mgcu.PREC_FP32),
                                                       (14, 0, 0, mgcu.PREC_FP32), (14, 13, 0, mgcu.PREC_MIXED),
-                                                      (14, 13, 512, mgcu.PREC_MIXED), (14, 13, 512, mgcu.PREC_FP64)])
+                                                      (14, 13, 512, mgcu.PREC_MIXED), (14, 13, 512, mgcu.PREC_FP64),
+                                                      (14, 12, 512, mgcu.PREC_MIXED), (12, 0, 512, mgcu.PREC_FP64)])
 def test_target_sweep_tiles_vs_oracle(lib, oracle, L, tile_bits, threads, prec):
     """the target-sweep kernel with 1, 2, 4 and 8 quartets per thread, one or several
     tiles per pass and structured and general gates (also on the dropped qubit), against
