@@ -432,14 +432,19 @@ __device__ __forceinline__ Gate8<T> load_gate(const T* m, int g)
 // the gate's cache column first
 template <class P>
 __device__ __forceinline__ void gate_forward(typename P::T* tile, const GateRec& r, const Gate8<typename P::T>& G, int Q, int tpar,
-	typename P::T* cache_g, const Smem& s, unsigned nlb)
+	typename P::T* cache_g, const Smem& s, unsigned nlb, bool tile_order = false)
 {
 	for (unsigned q = threadIdx.x; q < (unsigned)Q; q += blockDim.x)
 	{
 		unsigned ex, ew, ey, ez;
 		quartet(r, q, tpar, ex, ew, ey, ez);
 		const typename P::T x = tile[ex], w = tile[ew], y = tile[ey], z = tile[ez];
-		if (cache_g)
+		if (cache_g && tile_order)
+		{
+			// the cached state in tile order: the backward pass reads it back by local index
+			cache_g[ex] = x; cache_g[ew] = w; cache_g[ey] = y; cache_g[ez] = z;
+		}
+		else if (cache_g)
 		{
 			cache_g[gidx(s, nlb, ex)] = x; cache_g[gidx(s, nlb, ew)] = w;
 			cache_g[gidx(s, nlb, ey)] = y; cache_g[gidx(s, nlb, ez)] = z;
@@ -928,7 +933,10 @@ __device__ __forceinline__ void w_column(const Args<P>& a, long b, const typenam
 			dsrc = su;
 		}
 
-		// W forward, caching each gate's input; overlap on the last pass
+		// W forward, caching each gate's input; overlap on the last pass.  Without a
+		// Hessian (whose kernel reads the caches by global index) the cache of a gate is
+		// kept in tile order: tile tau of the gate's pass at offset tau * 2^kt
+		const bool tl = dcache == nullptr;
 		for (int p = 0; p < a.W.npass; p++)
 		{
 			const PassRec& pr = a.W.pass[p];
@@ -948,7 +956,8 @@ __device__ __forceinline__ void w_column(const Args<P>& a, long b, const typenam
 				{
 					const GateRec r = a.W.gate[gi];
 					const Gate8<T> G = load_gate(a.wm, r.g);
-					gate_forward<P>(tile, r, G, Q, tpar, cache ? cache + (size_t)r.g * S : nullptr, s, nlb);
+					gate_forward<P>(tile, r, G, Q, tpar, cache ? cache + (size_t)r.g * S + (tl ? ((size_t)tau << kt) : 0) : nullptr,
+						s, nlb, tl);
 					__syncthreads();
 				}
 				if (last)
@@ -986,6 +995,32 @@ __device__ __forceinline__ void w_column(const Args<P>& a, long b, const typenam
 					typename P::Acc acc[8];
 #pragma unroll
 					for (int e = 0; e < 8; e++) acc[e] = P::acc_zero();
+					if (tl && (unsigned)Q % blockDim.x == 0)
+					{
+						// cache in tile order, read one quartet ahead of the arithmetic
+						const T* ct = cg + ((size_t)tau << kt);
+						const unsigned nq = (unsigned)Q / blockDim.x;
+						unsigned ex, ew, ey, ez;
+						quartet(r, threadIdx.x, tpar, ex, ew, ey, ez);
+						T cx = ct[ex], cw = ct[ew], cy = ct[ey], cz = ct[ez];
+						for (unsigned k = 0; k < nq; k++)
+						{
+							const unsigned fx = ex, fw = ew, fy = ey, fz = ez;
+							const T x0 = cx, w0 = cw, y0 = cy, z0 = cz;
+							if (k + 1 < nq)
+							{
+								quartet(r, threadIdx.x + (k + 1) * blockDim.x, tpar, ex, ew, ey, ez);
+								cx = ct[ex]; cw = ct[ew]; cy = ct[ey]; cz = ct[ez];
+							}
+							const T dx = tile[fx], dw = tile[fw], dy = tile[fy], dz = tile[fz];
+							contract_quartet<P>(acc, dx, dw, dy, dz, x0, w0, y0, z0);
+							tile[fx] = P::madd2(G.k0, dx, G.k2, dw);
+							tile[fw] = P::madd2(G.k1, dx, G.k3, dw);
+							tile[fy] = P::madd2(G.c0, dy, G.c2, dz);
+							tile[fz] = P::madd2(G.c1, dy, G.c3, dz);
+						}
+					}
+					else
 					for (unsigned q = threadIdx.x; q < (unsigned)Q; q += blockDim.x)
 					{
 						unsigned ex, ew, ey, ez;
@@ -993,7 +1028,12 @@ __device__ __forceinline__ void w_column(const Args<P>& a, long b, const typenam
 						const unsigned gx = gidx(s, nlb, ex), gw = gidx(s, nlb, ew), gy = gidx(s, nlb, ey), gz = gidx(s, nlb, ez);
 						const T dx = tile[ex], dw = tile[ew], dy = tile[ey], dz = tile[ez];
 						if (dg) { dg[gx] = dx; dg[gw] = dw; dg[gy] = dy; dg[gz] = dz; }
-						contract_quartet<P>(acc, dx, dw, dy, dz, cg[gx], cg[gw], cg[gy], cg[gz]);
+						if (tl)
+						{
+							const T* ct = cg + ((size_t)tau << kt);
+							contract_quartet<P>(acc, dx, dw, dy, dz, ct[ex], ct[ew], ct[ey], ct[ez]);
+						}
+						else contract_quartet<P>(acc, dx, dw, dy, dz, cg[gx], cg[gw], cg[gy], cg[gz]);
 						// transpose (no conjugation): reference src/gate.c:725-728
 						tile[ex] = P::madd2(G.k0, dx, G.k2, dw);
 						tile[ew] = P::madd2(G.k1, dx, G.k3, dw);
@@ -1010,7 +1050,7 @@ __device__ __forceinline__ void w_column(const Args<P>& a, long b, const typenam
 }
 
 template <class P, bool WithU>
-__global__ void __launch_bounds__(256) k_columns(Args<P> a)
+__global__ void __launch_bounds__(256, 2) k_columns(Args<P> a)
 {
 	typedef typename P::T T;
 	extern __shared__ __align__(16) char smem_raw[];
