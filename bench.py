@@ -102,7 +102,7 @@ def workload(L, nlayers, nsteps, seed=3):
 # summarised in profiles/k_target_mixed_hubbard_L16.md (608 columns, L=16, mixed); the
 # kernel's traffic is its output columns plus tile round trips that miss L2, both
 # proportional to the number of columns, so per-launch traffic = this x columns per launch
-TARGET_DRAM_BYTES_PER_COLUMN = {16: (13.142094e9 + 14.298918e9) / 608}
+TARGET_DRAM_BYTES_PER_COLUMN = {16: (11.680262e9 + 12.663491e9) / 608}
 
 
 def alg_flops(L, gu, gw, ncols):
