@@ -933,10 +933,11 @@ __device__ __forceinline__ void w_column(const Args<P>& a, long b, const typenam
 			dsrc = su;
 		}
 
-		// W forward, caching each gate's input; overlap on the last pass.  Without a
-		// Hessian (whose kernel reads the caches by global index) the cache of a gate is
-		// kept in tile order: tile tau of the gate's pass at offset tau * 2^kt
-		const bool tl = dcache == nullptr;
+		// W forward, caching each gate's input; overlap on the last pass.  The caches of a
+		// gate (its input here, the derivative entering it in the backward sweep) are kept
+		// in tile order: tile tau of the gate's pass at offset tau * 2^kt, read back by
+		// local index in the backward sweep and by the Hessian items
+		const bool tl = true;
 		for (int p = 0; p < a.W.npass; p++)
 		{
 			const PassRec& pr = a.W.pass[p];
@@ -1013,6 +1014,11 @@ __device__ __forceinline__ void w_column(const Args<P>& a, long b, const typenam
 								cx = ct[ex]; cw = ct[ew]; cy = ct[ey]; cz = ct[ez];
 							}
 							const T dx = tile[fx], dw = tile[fw], dy = tile[fy], dz = tile[fz];
+							if (dg)
+							{
+								T* dt = dg + ((size_t)tau << kt);
+								dt[fx] = dx; dt[fw] = dw; dt[fy] = dy; dt[fz] = dz;
+							}
 							contract_quartet<P>(acc, dx, dw, dy, dz, x0, w0, y0, z0);
 							tile[fx] = P::madd2(G.k0, dx, G.k2, dw);
 							tile[fw] = P::madd2(G.k1, dx, G.k3, dw);
@@ -1027,7 +1033,11 @@ __device__ __forceinline__ void w_column(const Args<P>& a, long b, const typenam
 						quartet(r, q, tpar, ex, ew, ey, ez);
 						const unsigned gx = gidx(s, nlb, ex), gw = gidx(s, nlb, ew), gy = gidx(s, nlb, ey), gz = gidx(s, nlb, ez);
 						const T dx = tile[ex], dw = tile[ew], dy = tile[ey], dz = tile[ez];
-						if (dg) { dg[gx] = dx; dg[gw] = dw; dg[gy] = dy; dg[gz] = dz; }
+						if (dg)
+						{
+							T* dt = dg + ((size_t)tau << kt);
+							dt[ex] = dx; dt[ew] = dw; dt[ey] = dy; dt[ez] = dz;
+						}
 						if (tl)
 						{
 							const T* ct = cg + ((size_t)tau << kt);
@@ -1145,7 +1155,13 @@ __global__ void __launch_bounds__(256) k_hessian(Args<P> a, long nitems)
 			{
 				const unsigned nlb = nl_base(pr, tau);
 				const int tpar = (__popcll(nlb) + par) & 1;
-				tile_load<P>(tile, kt, s, nlb, (pp == pk) ? cache + (size_t)k * S : sh);
+				if (pp == pk)
+				{
+					// the placement gate's input, cached in tile order
+					const T* ct = cache + (size_t)k * S + ((size_t)tau << kt);
+					for (unsigned e = threadIdx.x; e < (1u << kt); e += blockDim.x) tile[e] = ct[e];
+				}
+				else tile_load<P>(tile, kt, s, nlb, sh);
 				__syncthreads();
 				for (int gi = pr.gbeg; gi < pr.gend; gi++)
 				{
@@ -1178,7 +1194,7 @@ __global__ void __launch_bounds__(256) k_hessian(Args<P> a, long nitems)
 						continue;
 					}
 					const Gate8<T> G = load_gate(a.wm, r.g);
-					const T* dg = dcache + (size_t)r.g * S;
+					const T* dg = dcache + (size_t)r.g * S + ((size_t)tau << kt);   // tile order
 					const bool apply = (r.g != a.ngates - 1);
 					typename P::Acc acc[8];
 #pragma unroll
@@ -1188,7 +1204,7 @@ __global__ void __launch_bounds__(256) k_hessian(Args<P> a, long nitems)
 						unsigned ex, ew, ey, ez;
 						quartet(r, q, tpar, ex, ew, ey, ez);
 						const T vx = tile[ex], vw = tile[ew], vy = tile[ey], vz = tile[ez];
-						contract_quartet<P>(acc, dg[gidx(s, nlb, ex)], dg[gidx(s, nlb, ew)], dg[gidx(s, nlb, ey)], dg[gidx(s, nlb, ez)], vx, vw, vy, vz);
+						contract_quartet<P>(acc, dg[ex], dg[ew], dg[ey], dg[ez], vx, vw, vy, vz);
 						if (apply)
 						{
 							tile[ex] = P::madd2(G.k0, vx, G.k1, vw);
