@@ -872,15 +872,6 @@ static void (*target_kernel(int kt, int threads))(Args<P>)
 	return k_target<P, 256, 0>;
 }
 
-// the same dispatch inside a kernel (batches: each item has its own tile size)
-template <class P>
-__device__ __forceinline__ void tgt_column_rt(const Args<P>& a, long b, typename P::T* out, char* smem_raw)
-{
-	const unsigned Q = 1u << (a.kt - 2);
-	if (Q == 4u * blockDim.x) tgt_column<P, 4>(a, b, out, smem_raw);
-	else if (Q == 8u * blockDim.x) tgt_column<P, 8>(a, b, out, smem_raw);
-	else tgt_column<P, 0>(a, b, out, smem_raw);
-}
 
 // ------------------------------------------------------------------------------------
 // batched launches: work items (instance, column range) of many instances, taken by
@@ -1080,10 +1071,11 @@ __global__ void __launch_bounds__(256, 2) k_columns(Args<P> a)
 	block_reduce1<P>(facc, s.red, a.part_f + (size_t)blockIdx.x * 2);
 }
 
-// batched items, target and fitted circuit per column: the target column goes into the
+// batched items of one tile class (quartets per thread in the target sweep: QPT), target
+// and fitted circuit per column: the target column goes into the
 // block's slot sx, then the fitted circuit runs against it; slots and gate cache live in
 // per-block scratch (3 slots of slot_stride, then cache_stride elements)
-template <class P>
+template <class P, int QPT>
 __global__ void __launch_bounds__(256, 2) k_batch(const Args<P>* __restrict__ args_t, const Args<P>* __restrict__ args_c,
 	const BatchItem* __restrict__ items, int nitems, int* counter, typename P::T* scratch, long slot_stride, long cache_stride)
 {
@@ -1104,7 +1096,7 @@ __global__ void __launch_bounds__(256, 2) k_batch(const Args<P>* __restrict__ ar
 		typename P::Acc facc = P::acc_zero();
 		for (long b = I.b0; b < I.b1; b++)
 		{
-			tgt_column_rt<P>(at, b, sx, smem_raw);
+			tgt_column<P, QPT>(at, b, sx, smem_raw);
 			w_column<P, false>(a, b, sx, b, I.slot, su, sw, a.want_grad ? cache : nullptr, nullptr, facc, smem_raw);
 		}
 		T* tile;
@@ -2205,7 +2197,8 @@ struct mgcu_batch
 	DevBuf args_t, args_c, items, counters, scratch, parts, red;
 	long slot_stride = 0, cache_stride = 0;
 	size_t smem = 0;
-	int grid = 0, nitems = 0;
+	int grid[3] = { 0, 0, 0 }, nitems = 0;
+	int class_beg[4] = { 0, 0, 0, 0 };   // items of tile classes 4, 8, any quartets per thread
 	long graph_kernels = 0;        // kernel nodes per replay
 	bool use_graph = true;         // false: plain launches (a batch run once)
 	cudaGraph_t graph = nullptr;
@@ -2324,17 +2317,26 @@ static int batch_build(mgcu_batch* B, const mgcu_batch_inst* d, int tune)
 		B->slot_stride = std::max(B->slot_stride, I.S);
 		if (D.want_grad) B->cache_stride = std::max(B->cache_stride, I.S * D.ngates);
 	}
-	// the batched kernel also holds one static shared int: ask for exactly what it uses
-	MGCU_TRY(cudaFuncSetAttribute(k_batch<P>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)B->smem));
-	int pb = 0;
-	MGCU_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&pb, k_batch<P>, threads, B->smem));
-	if (pb < 1) { mg_set_error("batch: a block does not fit on an SM"); return MG_ERR_ARG; }
-	B->grid = c->nsm * pb;
+	// one batched kernel per tile class; each also holds one static shared int: ask for
+	// exactly what it uses
+	void (*const kb[3])(const Args<P>*, const Args<P>*, const BatchItem*, int, int*, T*, long, long) = { k_batch<P, 4>, k_batch<P, 8>, k_batch<P, 0> };
+	for (int k = 0; k < 3; k++)
+	{
+		MGCU_TRY(cudaFuncSetAttribute(kb[k], cudaFuncAttributeMaxDynamicSharedMemorySize, (int)B->smem));
+		int pb = 0;
+		MGCU_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&pb, kb[k], threads, B->smem));
+		if (pb < 1) { mg_set_error("batch: a block does not fit on an SM"); return MG_ERR_ARG; }
+		B->grid[k] = c->nsm * pb;
+	}
+	auto tile_class = [&](const BatchInst& I) {
+		const long Q = 1L << (I.kt_t - 2);
+		return (Q == 4L * threads) ? 0 : (Q == 8L * threads) ? 1 : 2;
+	};
 
 	// work items: about 16 per block, never more than an instance's columns, largest first
 	double total = 0;
 	for (int i = 0; i < B->n; i++) total += B->inst[i].col_cost * (double)(1L << B->inst[i].L);
-	const double item_cost = total / (16.0 * B->grid);
+	const double item_cost = total / (16.0 * B->grid[0]);
 	struct HostItem { BatchItem it; double cost; };
 	std::vector<HostItem> all;
 	for (int i = 0; i < B->n; i++)
@@ -2350,7 +2352,23 @@ static int batch_build(mgcu_batch* B, const mgcu_batch_inst* d, int tune)
 			all.push_back(h);
 		}
 	}
-	std::stable_sort(all.begin(), all.end(), [](const HostItem& x, const HostItem& y) { return x.cost > y.cost; });
+	// by tile class, then largest first
+	std::vector<int> cls(B->n);
+	for (int i = 0; i < B->n; i++) cls[i] = tile_class(B->inst[i]);
+	std::stable_sort(all.begin(), all.end(), [&](const HostItem& x, const HostItem& y) {
+		const int cx = cls[x.it.inst], cy = cls[y.it.inst];
+		return cx != cy ? cx < cy : x.cost > y.cost;
+	});
+	for (int k = 0; k <= 3; k++) B->class_beg[k] = 0;
+	{
+		int n = 0;
+		for (int k = 0; k < 3; k++)
+		{
+			B->class_beg[k] = n;
+			for (const HostItem& h : all) if (cls[h.it.inst] == k) n++;
+		}
+		B->class_beg[3] = n;
+	}
 	std::vector<BatchItem> items;
 	for (const HostItem& h : all) items.push_back(h.it);
 	B->nitems = (int)items.size();
@@ -2364,9 +2382,10 @@ static int batch_build(mgcu_batch* B, const mgcu_batch_inst* d, int tune)
 		I.part_g_off = off; off += 16L * I.nslots * std::max(I.ngates, 1);
 	}
 	int e = B->parts.alloc(sizeof(double) * std::max(off, 1L));
-	if (!e) e = B->scratch.alloc(sizeof(T) * (size_t)B->grid * (size_t)(3 * B->slot_stride + B->cache_stride));
+	const int gmax = std::max(B->grid[0], std::max(B->grid[1], B->grid[2]));
+	if (!e) e = B->scratch.alloc(sizeof(T) * (size_t)gmax * (size_t)(3 * B->slot_stride + B->cache_stride));
 	if (!e) e = B->items.alloc(sizeof(BatchItem) * std::max<size_t>(items.size(), 1));
-	if (!e) e = B->counters.alloc(sizeof(int) * 2);
+	if (!e) e = B->counters.alloc(sizeof(int) * 4);
 	if (!e) e = B->args_t.alloc(sizeof(Args<P>) * B->n);
 	if (!e) e = B->args_c.alloc(sizeof(Args<P>) * B->n);
 	if (!e) e = B->red.alloc(sizeof(BatchRed) * B->n);
@@ -2408,9 +2427,15 @@ static int batch_issue(mgcu_batch* B)
 	cudaStream_t st = mgcu_ctx()->stream;
 	MGCU_TRY(cudaMemsetAsync(B->parts.p, 0, B->parts.n, st));
 	MGCU_TRY(cudaMemsetAsync(B->counters.p, 0, B->counters.n, st));
-	k_batch<P><<<std::min(B->grid, B->nitems), B->threads, B->smem, st>>>(B->args_t.as<Args<P>>(), B->args_c.as<Args<P>>(),
-		B->items.as<BatchItem>(), B->nitems, B->counters.as<int>(), B->scratch.as<T>(), B->slot_stride, B->cache_stride);
-	MGCU_LAUNCHED();
+	void (*const kb[3])(const Args<P>*, const Args<P>*, const BatchItem*, int, int*, T*, long, long) = { k_batch<P, 4>, k_batch<P, 8>, k_batch<P, 0> };
+	for (int k = 0; k < 3; k++)
+	{
+		const int i0 = B->class_beg[k], ni = B->class_beg[k + 1] - i0;
+		if (ni == 0) continue;
+		kb[k]<<<std::min(B->grid[k], ni), B->threads, B->smem, st>>>(B->args_t.as<Args<P>>(), B->args_c.as<Args<P>>(),
+			B->items.as<BatchItem>() + i0, ni, B->counters.as<int>() + k, B->scratch.as<T>(), B->slot_stride, B->cache_stride);
+		MGCU_LAUNCHED();
+	}
 	k_batch_reduce<<<B->n, 128, 0, st>>>(B->red.as<BatchRed>());
 	MGCU_LAUNCHED();
 	return 0;
