@@ -597,111 +597,129 @@ __host__ __device__ __forceinline__ unsigned tsw(unsigned e)
 }
 
 
-// one 2x2 block on QPT pairs (slots x ^ m0, x ^ m1); SG: off-diagonal entries negated
-// on the pairs with sg[k] == 1 (implemented by negating the off-diagonal inputs)
-template <class P, int QPT, bool SG>
-__device__ __forceinline__ void tgt_block(char* tb, const unsigned (&x)[QPT], unsigned m0, unsigned m1, int kind, unsigned rot,
-	const typename P::T* m, const unsigned (&sg)[QPT])
+// one 2x2 block on QPT pairs (slots x ^ m0, x ^ m1) of NC tiles td bytes apart (NC
+// columns of equal parity sharing every index); SG: off-diagonal entries negated on the
+// pairs with sg[k] == 1 (implemented by negating the off-diagonal inputs)
+template <class P, int QPT, bool SG, int NC>
+__device__ __forceinline__ void tgt_block(char* tb, unsigned td, const unsigned (&x)[QPT], unsigned m0, unsigned m1, int kind,
+	unsigned rot, const typename P::T* m, const unsigned (&sg)[QPT])
 {
 	typedef typename P::T T;
-	T a[QPT], b[QPT];
+	T a[NC][QPT], b[NC][QPT];
+#define TGT_A(c, k) (*(T*)(tb + (c) * td + (x[k] ^ m0)))
+#define TGT_B(c, k) (*(T*)(tb + (c) * td + (x[k] ^ m1)))
+#define TGT_LOAD_AB() _Pragma("unroll") for (int c = 0; c < NC; c++) _Pragma("unroll") for (int k = 0; k < QPT; k++) { a[c][k] = TGT_A(c, k); b[c][k] = TGT_B(c, k); }
+#define TGT_LOAD_B() _Pragma("unroll") for (int c = 0; c < NC; c++) _Pragma("unroll") for (int k = 0; k < QPT; k++) b[c][k] = TGT_B(c, k);
 	switch (kind)
 	{
 	case BK_ID: return;
 	case BK_SWAP:
+		TGT_LOAD_AB()
 #pragma unroll
-		for (int k = 0; k < QPT; k++) { a[k] = *(T*)(tb + (x[k] ^ m0)); b[k] = *(T*)(tb + (x[k] ^ m1)); }
+		for (int c = 0; c < NC; c++)
 #pragma unroll
-		for (int k = 0; k < QPT; k++)
-		{
-			*(T*)(tb + (x[k] ^ m0)) = SG ? P::negif(b[k], sg[k]) : b[k];
-			*(T*)(tb + (x[k] ^ m1)) = SG ? P::negif(a[k], sg[k]) : a[k];
-		}
+			for (int k = 0; k < QPT; k++)
+			{
+				TGT_A(c, k) = SG ? P::negif(b[c][k], sg[k]) : b[c][k];
+				TGT_B(c, k) = SG ? P::negif(a[c][k], sg[k]) : a[c][k];
+			}
 		return;
 	case BK_NEG1:
+		TGT_LOAD_B()
 #pragma unroll
-		for (int k = 0; k < QPT; k++) b[k] = *(T*)(tb + (x[k] ^ m1));
+		for (int c = 0; c < NC; c++)
 #pragma unroll
-		for (int k = 0; k < QPT; k++) *(T*)(tb + (x[k] ^ m1)) = P::neg(b[k]);
+			for (int k = 0; k < QPT; k++) TGT_B(c, k) = P::neg(b[c][k]);
 		return;
 	case BK_D1:
 	{
 		const T c3 = m[3];
+		TGT_LOAD_B()
 #pragma unroll
-		for (int k = 0; k < QPT; k++) b[k] = *(T*)(tb + (x[k] ^ m1));
+		for (int c = 0; c < NC; c++)
 #pragma unroll
-		for (int k = 0; k < QPT; k++) *(T*)(tb + (x[k] ^ m1)) = P::mul(c3, b[k]);
+			for (int k = 0; k < QPT; k++) TGT_B(c, k) = P::mul(c3, b[c][k]);
 		return;
 	}
 	case BK_DIAG:
 	{
 		const T c0 = m[0], c3 = m[3];
+		TGT_LOAD_AB()
 #pragma unroll
-		for (int k = 0; k < QPT; k++) { a[k] = *(T*)(tb + (x[k] ^ m0)); b[k] = *(T*)(tb + (x[k] ^ m1)); }
+		for (int c = 0; c < NC; c++)
 #pragma unroll
-		for (int k = 0; k < QPT; k++) { *(T*)(tb + (x[k] ^ m0)) = P::mul(c0, a[k]); *(T*)(tb + (x[k] ^ m1)) = P::mul(c3, b[k]); }
+			for (int k = 0; k < QPT; k++) { TGT_A(c, k) = P::mul(c0, a[c][k]); TGT_B(c, k) = P::mul(c3, b[c][k]); }
 		return;
 	}
 	case BK_ANTI:
 	{
 		const T c1 = m[1], c2 = m[2];
+		TGT_LOAD_AB()
 #pragma unroll
-		for (int k = 0; k < QPT; k++) { a[k] = *(T*)(tb + (x[k] ^ m0)); b[k] = *(T*)(tb + (x[k] ^ m1)); }
+		for (int c = 0; c < NC; c++)
 #pragma unroll
-		for (int k = 0; k < QPT; k++)
-		{
-			if (SG) { a[k] = P::negif(a[k], sg[k]); b[k] = P::negif(b[k], sg[k]); }
-			*(T*)(tb + (x[k] ^ m0)) = P::mul(c1, b[k]); *(T*)(tb + (x[k] ^ m1)) = P::mul(c2, a[k]);
-		}
+			for (int k = 0; k < QPT; k++)
+			{
+				const T as = SG ? P::negif(a[c][k], sg[k]) : a[c][k], bs = SG ? P::negif(b[c][k], sg[k]) : b[c][k];
+				TGT_A(c, k) = P::mul(c1, bs); TGT_B(c, k) = P::mul(c2, as);
+			}
 		return;
 	}
 	case BK_RI:
 	{
 		const T c0 = m[0], c1 = m[1], c2 = m[2], c3 = m[3];
-#pragma unroll
-		for (int k = 0; k < QPT; k++) { a[k] = *(T*)(tb + (x[k] ^ m0)); b[k] = *(T*)(tb + (x[k] ^ m1)); }
+		TGT_LOAD_AB()
 		if (rot == 6u)   // real diagonal, imaginary off-diagonal (hopping terms)
 		{
 #pragma unroll
-			for (int k = 0; k < QPT; k++)
-			{
-				const T bs = SG ? P::negif(b[k], sg[k]) : b[k], as = SG ? P::negif(a[k], sg[k]) : a[k];
-				*(T*)(tb + (x[k] ^ m0)) = P::madd2_ri(c0, false, a[k], c1, true, bs);
-				*(T*)(tb + (x[k] ^ m1)) = P::madd2_ri(c2, true, as, c3, false, b[k]);
-			}
+			for (int c = 0; c < NC; c++)
+#pragma unroll
+				for (int k = 0; k < QPT; k++)
+				{
+					const T bs = SG ? P::negif(b[c][k], sg[k]) : b[c][k], as = SG ? P::negif(a[c][k], sg[k]) : a[c][k];
+					TGT_A(c, k) = P::madd2_ri(c0, false, a[c][k], c1, true, bs);
+					TGT_B(c, k) = P::madd2_ri(c2, true, as, c3, false, b[c][k]);
+				}
 		}
 		else
 		{
 #pragma unroll
-			for (int k = 0; k < QPT; k++)
-			{
-				const T bs = SG ? P::negif(b[k], sg[k]) : b[k], as = SG ? P::negif(a[k], sg[k]) : a[k];
-				*(T*)(tb + (x[k] ^ m0)) = P::madd2_ri(c0, rot & 1, a[k], c1, rot & 2, bs);
-				*(T*)(tb + (x[k] ^ m1)) = P::madd2_ri(c2, rot & 4, as, c3, rot & 8, b[k]);
-			}
+			for (int c = 0; c < NC; c++)
+#pragma unroll
+				for (int k = 0; k < QPT; k++)
+				{
+					const T bs = SG ? P::negif(b[c][k], sg[k]) : b[c][k], as = SG ? P::negif(a[c][k], sg[k]) : a[c][k];
+					TGT_A(c, k) = P::madd2_ri(c0, rot & 1, a[c][k], c1, rot & 2, bs);
+					TGT_B(c, k) = P::madd2_ri(c2, rot & 4, as, c3, rot & 8, b[c][k]);
+				}
 		}
 		return;
 	}
 	default:
 	{
 		const T c0 = m[0], c1 = m[1], c2 = m[2], c3 = m[3];
+		TGT_LOAD_AB()
 #pragma unroll
-		for (int k = 0; k < QPT; k++) { a[k] = *(T*)(tb + (x[k] ^ m0)); b[k] = *(T*)(tb + (x[k] ^ m1)); }
+		for (int c = 0; c < NC; c++)
 #pragma unroll
-		for (int k = 0; k < QPT; k++)
-		{
-			const T bs = SG ? P::negif(b[k], sg[k]) : b[k], as = SG ? P::negif(a[k], sg[k]) : a[k];
-			*(T*)(tb + (x[k] ^ m0)) = P::madd2(c0, a[k], c1, bs);
-			*(T*)(tb + (x[k] ^ m1)) = P::madd2(c2, as, c3, b[k]);
-		}
+			for (int k = 0; k < QPT; k++)
+			{
+				const T bs = SG ? P::negif(b[c][k], sg[k]) : b[c][k], as = SG ? P::negif(a[c][k], sg[k]) : a[c][k];
+				TGT_A(c, k) = P::madd2(c0, a[c][k], c1, bs);
+				TGT_B(c, k) = P::madd2(c2, as, c3, b[c][k]);
+			}
 	}
 	}
+#undef TGT_A
+#undef TGT_B
+#undef TGT_LOAD_AB
+#undef TGT_LOAD_B
 }
 
 // one target gate on the tile: QPT quartets per thread, q = t + k * blockDim.x
 // (QPT * blockDim.x == number of quartets); nlb: the tile's nonlocal compact bits
-template <class P, int QPT>
-__device__ __forceinline__ void tgt_gate(char* tb, const TGate& r, const typename P::T* mats, int tpar, unsigned nlb)
+template <class P, int QPT, int NC>
+__device__ __forceinline__ void tgt_gate(char* tb, unsigned td, const TGate& r, const typename P::T* mats, int tpar, unsigned nlb)
 {
 	constexpr int ES = sizeof(typename P::T);
 	const unsigned MW = r.m.x, MY = r.m.y, MZ = r.m.z, SCX = r.m.w;
@@ -733,22 +751,23 @@ __device__ __forceinline__ void tgt_gate(char* tb, const TGate& r, const typenam
 #pragma unroll
 		for (int k = 0; k < QPT; k++)
 			sg[k] = (s0 ^ ((k & 1) ? sp : 0u) ^ ((k & 2) ? (sp >> 1) : 0u) ^ ((k & 4) ? (sp >> 2) : 0u)) & 1u;
-		tgt_block<P, QPT, true>(tb, x, 0u, MW, (kw >> 3) & 7, (kw >> 10) & 15, m + 4, sg);
+		tgt_block<P, QPT, true, NC>(tb, td, x, 0u, MW, (kw >> 3) & 7, (kw >> 10) & 15, m + 4, sg);
 #pragma unroll
 		for (int k = 0; k < QPT; k++) sg[k] ^= md;
-		tgt_block<P, QPT, true>(tb, x, MY, MZ, kw & 7, (kw >> 6) & 15, m, sg);
+		tgt_block<P, QPT, true, NC>(tb, td, x, MY, MZ, kw & 7, (kw >> 6) & 15, m, sg);
 	}
 	else
 	{
-		tgt_block<P, QPT, false>(tb, x, 0u, MW, (kw >> 3) & 7, (kw >> 10) & 15, m + 4, sg);
-		tgt_block<P, QPT, false>(tb, x, MY, MZ, kw & 7, (kw >> 6) & 15, m, sg);
+		tgt_block<P, QPT, false, NC>(tb, td, x, 0u, MW, (kw >> 3) & 7, (kw >> 10) & 15, m + 4, sg);
+		tgt_block<P, QPT, false, NC>(tb, td, x, MY, MZ, kw & 7, (kw >> 6) & 15, m, sg);
 	}
 }
 
 // the same with one quartet per iteration, for tiles whose quartet count is not 4 or 8
 // times the block size
-template <class P>
-__device__ __forceinline__ void tgt_gate_any(char* tb, const TGate& r, const typename P::T* mats, int tpar, unsigned nlb, unsigned Q)
+template <class P, int NC>
+__device__ __forceinline__ void tgt_gate_any(char* tb, unsigned td, const TGate& r, const typename P::T* mats, int tpar, unsigned nlb,
+	unsigned Q)
 {
 	constexpr int ES = sizeof(typename P::T);
 	const unsigned MW = r.m.x, MY = r.m.y, MZ = r.m.z, SCX = r.m.w;
@@ -764,63 +783,70 @@ __device__ __forceinline__ void tgt_gate_any(char* tb, const TGate& r, const typ
 		const unsigned x[1] = { (tsw<ES>(e) * ES) ^ (pe ? SCX : 0u) };
 		const unsigned sgk[1] = { ((unsigned)__popc(e & ml) + sn + (md ? pe : 0u)) & 1u };
 		const unsigned sgc[1] = { sgk[0] ^ md };
-		tgt_block<P, 1, true>(tb, x, 0u, MW, (kw >> 3) & 7, (kw >> 10) & 15, m + 4, sgk);
-		tgt_block<P, 1, true>(tb, x, MY, MZ, kw & 7, (kw >> 6) & 15, m, sgc);
+		tgt_block<P, 1, true, NC>(tb, td, x, 0u, MW, (kw >> 3) & 7, (kw >> 10) & 15, m + 4, sgk);
+		tgt_block<P, 1, true, NC>(tb, td, x, MY, MZ, kw & 7, (kw >> 6) & 15, m, sgc);
 	}
 }
 
 // the gates [gbeg, gend) of a pass on one tile, records read one gate ahead
-template <class P, int QPT>
-__device__ __forceinline__ void tgt_gates(char* tb, const TGate* gates, int gbeg, int gend, const typename P::T* mats, int tpar,
-	unsigned nlb, unsigned Q)
+template <class P, int QPT, int NC>
+__device__ __forceinline__ void tgt_gates(char* tb, unsigned td, const TGate* gates, int gbeg, int gend, const typename P::T* mats,
+	int tpar, unsigned nlb, unsigned Q)
 {
 	if (gbeg >= gend) return;
 	TGate r = gates[gbeg];
 	for (int gi = gbeg; gi < gend; gi++)
 	{
 		const TGate rn = gates[min(gi + 1, gend - 1)];
-		if (QPT > 0) tgt_gate<P, (QPT > 0 ? QPT : 1)>(tb, r, mats, tpar, nlb);
-		else tgt_gate_any<P>(tb, r, mats, tpar, nlb, Q);
+		if (QPT > 0) tgt_gate<P, (QPT > 0 ? QPT : 1), NC>(tb, td, r, mats, tpar, nlb);
+		else tgt_gate_any<P, NC>(tb, td, r, mats, tpar, nlb, Q);
 		__syncthreads();
 		r = rn;
 	}
 }
 
-// -conj(U e_b) of one basis column b into out (the whole block); QPT: quartets per
-// thread and gate (0: any, one quartet per iteration)
-template <class P, int QPT>
-__device__ __forceinline__ void tgt_column(const Args<P>& a, long b, typename P::T* out, char* smem_raw)
+// -conj(U e_b) of NC basis columns bs (of equal parity) into outs (the whole block); QPT:
+// quartets per thread and gate (0: any, one quartet per iteration).  Shared memory: NC
+// tiles, then the deposit tables and scratch; the pass matrices at a.pm_off.
+template <class P, int QPT, int NC>
+__device__ __forceinline__ void tgt_column(const Args<P>& a, const long (&bs)[NC], typename P::T* const (&outs)[NC], char* smem_raw)
 {
 	typedef typename P::T T;
 	constexpr int ES = sizeof(T);
-	T* tile;
-	Smem s = smem_layout<T>(smem_raw, a.kt, tile);
-	char* tb = reinterpret_cast<char*>(tile);
-	T* pm = reinterpret_cast<T*>(smem_raw + a.pm_off);   // this pass's distinct matrices
 	const int kt = a.kt;
-	const unsigned n = 1u << kt, Q = n >> 2;
+	const unsigned n = 1u << kt, Q = n >> 2, td = n * ES;
+	T* tile_last;
+	Smem s = smem_layout<T>(smem_raw + (NC - 1) * td, kt, tile_last);
+	char* tb = smem_raw;
+	T* pm = reinterpret_cast<T*>(smem_raw + a.pm_off);   // this pass's distinct matrices
+	const int par = __popcll(bs[0]) & 1;
+	for (int p = 0; p < a.U.npass; p++)
 	{
-		const int par = __popcll(b) & 1;
-		const unsigned cb = (unsigned)(b >> 1);
-		for (int p = 0; p < a.U.npass; p++)
+		const PassRec& pr = a.U.pass[p];
+		__syncthreads();
+		setup_pass(pr, kt, s);
 		{
-			const PassRec& pr = a.U.pass[p];
-			__syncthreads();
-			setup_pass(pr, kt, s);
+			const int2 mp = a.upm[p];
+			for (int i = threadIdx.x; i < mp.y * 8; i += blockDim.x) pm[i] = a.upmats[mp.x + i];
+		}
+		__syncthreads();
+		const bool last = p == a.U.npass - 1;
+		const unsigned ntile = 1u << pr.nnl;
+		for (unsigned tau = 0; tau < ntile; tau++)
+		{
+			const unsigned nlb = nl_base(pr, tau);
+			const int tpar = (__popc(nlb) + par) & 1;
+#pragma unroll
+			for (int c = 0; c < NC; c++)
 			{
-				const int2 mp = a.upm[p];
-				for (int i = threadIdx.x; i < mp.y * 8; i += blockDim.x) pm[i] = a.upmats[mp.x + i];
-			}
-			__syncthreads();
-			const bool last = p == a.U.npass - 1;
-			const unsigned ntile = 1u << pr.nnl;
-			for (unsigned tau = 0; tau < ntile; tau++)
-			{
-				const unsigned nlb = nl_base(pr, tau);
-				const int tpar = (__popc(nlb) + par) & 1;
+				T* tile = reinterpret_cast<T*>(tb + c * td);
+				const T* out = outs[c];
 				if (p == 0)
+				{
+					const unsigned cb = (unsigned)(bs[c] >> 1);
 					for (unsigned e = threadIdx.x; e < n; e += blockDim.x)
 						tile[tsw<ES>(e)] = (gidx(s, nlb, e) == cb) ? P::make(1.0, 0.0) : P::zero();
+				}
 				else
 					for (unsigned e0 = threadIdx.x; e0 < n; e0 += 8 * blockDim.x)
 					{
@@ -838,17 +864,31 @@ __device__ __forceinline__ void tgt_column(const Args<P>& a, long b, typename P:
 							if (e < n) tile[tsw<ES>(e)] = v[k];
 						}
 					}
-				__syncthreads();
-				tgt_gates<P, QPT>(tb, a.utg, pr.gbeg, pr.gend, pm, tpar, nlb, Q);
+			}
+			__syncthreads();
+			tgt_gates<P, QPT, NC>(tb, td, a.utg, pr.gbeg, pr.gend, pm, tpar, nlb, Q);
+#pragma unroll
+			for (int c = 0; c < NC; c++)
+			{
+				const T* tile = reinterpret_cast<const T*>(tb + c * td);
+				T* out = outs[c];
 				for (unsigned e = threadIdx.x; e < n; e += blockDim.x)
 				{
 					const T v = tile[tsw<ES>(e)];
 					out[gidx(s, nlb, e)] = last ? P::negconj(v) : v;
 				}
-				__syncthreads();
 			}
+			__syncthreads();
 		}
 	}
+}
+
+template <class P, int QPT>
+__device__ __forceinline__ void tgt_column(const Args<P>& a, long b, typename P::T* out, char* smem_raw)
+{
+	const long bs[1] = { b };
+	typename P::T* const outs[1] = { out };
+	tgt_column<P, QPT, 1>(a, bs, outs, smem_raw);
 }
 
 // one instantiation per (block size, quartets per thread), so that each keeps only its
@@ -861,11 +901,39 @@ __global__ void __launch_bounds__(NT, (NT == 512 && QPT == 4) ? 1 : 2) k_target(
 		tgt_column<P, QPT>(a, b, a.ucols + (size_t)(b - a.b0) * a.S, smem_raw);
 }
 
-// the k_target instantiation for a tile of 2^kt amplitudes and a block size
+// two columns of equal parity per block (b, b ^ 3 within each aligned group of four),
+// sharing every per-gate computation; columns outside whole groups one at a time
+template <class P, int QPT>
+__global__ void __launch_bounds__(256, 1) k_target2(Args<P> a)
+{
+	typedef typename P::T T;
+	extern __shared__ __align__(16) char smem_raw[];
+	const long g0 = (a.b0 + 3) >> 2, g1 = a.b1 >> 2;
+	const long npair = g1 > g0 ? 2 * (g1 - g0) : 0;
+	for (long j = blockIdx.x; j < npair; j += gridDim.x)
+	{
+		const long base = (g0 + (j >> 1)) << 2;
+		const long bs[2] = { base + (j & 1), base + 3 - (j & 1) };
+		T* const outs[2] = { a.ucols + (size_t)(bs[0] - a.b0) * a.S, a.ucols + (size_t)(bs[1] - a.b0) * a.S };
+		tgt_column<P, QPT, 2>(a, bs, outs, smem_raw);
+	}
+	// the rest: [b0, 4 g0) and [4 g1, b1), or all of [b0, b1) without a whole group
+	const long r0 = npair ? min(a.b1, g0 << 2) - a.b0 : a.b1 - a.b0;
+	const long r1 = npair ? a.b1 - (g1 << 2) : 0;
+	for (long j = (long)gridDim.x - 1 - blockIdx.x; j < r0 + r1; j += gridDim.x)
+	{
+		const long b = j < r0 ? a.b0 + j : (g1 << 2) + (j - r0);
+		tgt_column<P, QPT>(a, b, a.ucols + (size_t)(b - a.b0) * a.S, smem_raw);
+	}
+}
+
+// the k_target instantiation for a tile of 2^kt amplitudes, a block size and columns per
+// block (2: k_target2, 256 threads)
 template <class P>
-static void (*target_kernel(int kt, int threads))(Args<P>)
+static void (*target_kernel(int kt, int threads, int nc = 1))(Args<P>)
 {
 	const long q = (1L << (kt - 2)) / threads, exact = (1L << (kt - 2)) % threads == 0;
+	if (nc == 2) return (exact && q == 4) ? k_target2<P, 4> : (exact && q == 8) ? k_target2<P, 8> : k_target2<P, 0>;
 	if (threads > 256) return (exact && q == 2) ? k_target<P, 512, 2> : (exact && q == 4) ? k_target<P, 512, 4> : k_target<P, 512, 0>;
 	if (exact && q == 4) return k_target<P, 256, 4>;
 	if (exact && q == 8) return k_target<P, 256, 8>;
@@ -1717,7 +1785,7 @@ struct mgcu_plan
 	std::vector<int> wires, block, place;
 	std::vector<double> place_w;
 	int L, nb, kt, threads, grid_a, grid_b, grid_t, prec;
-	int kt_t, threads_t;           // k_target's tile bits and block size
+	int kt_t, threads_t, nc_t;     // k_target's tile bits, block size and columns per block
 	size_t smem_t;                 // k_target: its tile, tables, scratch and MAXPM staged matrices
 	bool ktime = false;            // record events around k_target launches (mgcu_plan_time_ms)
 	std::vector<cudaEvent_t> kev;  // start/stop pairs
@@ -1756,7 +1824,7 @@ static int launch_target(mgcu_plan* p, long b0, long b1, typename P::T* out)
 	a.pm_off = (unsigned)(p->smem_t - (size_t)MAXPM * 8 * p->tsize);
 	a.b0 = b0; a.b1 = b1;
 	a.ucols = out;
-	const int grid = (int)std::min<long>(p->grid_t, b1 - b0);
+	const int grid = (int)std::min<long>(p->grid_t, p->nc_t == 2 ? std::max(1L, (b1 - b0 + 1) / 2) : b1 - b0);
 	if (p->ktime)
 		while (p->kev.size() < p->kev_used + 2)
 		{
@@ -1765,7 +1833,7 @@ static int launch_target(mgcu_plan* p, long b0, long b1, typename P::T* out)
 			p->kev.push_back(ev);
 		}
 	if (p->ktime) MGCU_TRY(cudaEventRecord(p->kev[p->kev_used], c->stream));
-	void (*kern)(Args<P>) = target_kernel<P>(p->kt_t, p->threads_t);
+	void (*kern)(Args<P>) = target_kernel<P>(p->kt_t, p->threads_t, p->nc_t);
 	if (!kern) { mg_set_error("no target-sweep kernel for 2^%d amplitudes and %d threads", p->kt_t, p->threads_t); return MG_ERR_ARG; }
 	kern<<<grid, p->threads_t, p->smem_t, c->stream>>>(a);
 	MGCU_LAUNCHED();
@@ -1817,20 +1885,20 @@ static int set_smem_attr()
 {
 	MgcuContext* c = mgcu_ctx();
 	MGCU_TRY(cudaFuncSetAttribute(k_columns<P, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)std::min<size_t>(c->smem_optin, 227 * 1024)));
-	void (*const tk[6])(Args<P>) = { k_target<P, 256, 4>, k_target<P, 256, 8>, k_target<P, 256, 0>, k_target<P, 512, 2>,
-		k_target<P, 512, 4>, k_target<P, 512, 0> };
+	void (*const tk[9])(Args<P>) = { k_target<P, 256, 4>, k_target<P, 256, 8>, k_target<P, 256, 0>, k_target<P, 512, 2>,
+		k_target<P, 512, 4>, k_target<P, 512, 0>, k_target2<P, 4>, k_target2<P, 8>, k_target2<P, 0> };
 	for (auto k : tk) MGCU_TRY(cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)std::min<size_t>(c->smem_optin, 227 * 1024)));
 	MGCU_TRY(cudaFuncSetAttribute(k_hessian<P>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)std::min<size_t>(c->smem_optin, 227 * 1024)));
 	return 0;
 }
 
 template <class P>
-static int occupancy(int threads, size_t smem, int kt_t, int threads_t, size_t smem_t, int& per_sm, int& per_sm_target)
+static int occupancy(int threads, size_t smem, int kt_t, int threads_t, int nc_t, size_t smem_t, int& per_sm, int& per_sm_target)
 {
 	int n1 = 0, n2 = 0, n3 = 0;
 	MGCU_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n1, k_columns<P, false>, threads, smem));
 	MGCU_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n2, k_hessian<P>, threads, smem));
-	void (*kern)(Args<P>) = target_kernel<P>(kt_t, threads_t);
+	void (*kern)(Args<P>) = target_kernel<P>(kt_t, threads_t, nc_t);
 	if (!kern) { mg_set_error("no target-sweep kernel for 2^%d amplitudes and %d threads", kt_t, threads_t); return MG_ERR_ARG; }
 	MGCU_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n3, kern, threads_t, smem_t));
 	per_sm = std::max(1, std::min(n1, n2));
@@ -1897,13 +1965,14 @@ extern "C" mgcu_plan* mgcu_plan_create(const mgcu_plan_desc* d)
 		const long ot = mgcu_option(MG_OPT_TARGET_THREADS_ID);
 		if (ot > 0) tt = (int)std::max(32L, std::min(512L, (ot / 32) * 32));
 		p->threads_t = tt;
-		p->smem_t = ((size_t)1 << p->kt_t) * p->tsize + 2 * 128 * sizeof(unsigned)
+		p->nc_t = (mgcu_option(MG_OPT_TARGET_COLUMNS_ID) == 2 && tt == 256) ? 2 : 1;
+		p->smem_t = (size_t)p->nc_t * ((size_t)1 << p->kt_t) * p->tsize + 2 * 128 * sizeof(unsigned)
 			+ std::max<size_t>((size_t)(tt / 32) * 16 * sizeof(double), 16 * 16) + (size_t)MAXPM * 8 * p->tsize;
 	}
 	int per_sm = 1, per_sm_t = 1, e = 0;
-	if (p->prec == MG_PREC_FP64_ID) { e = set_smem_attr<PrecD>(); if (!e) e = occupancy<PrecD>(threads, p->smem, p->kt_t, p->threads_t, p->smem_t, per_sm, per_sm_t); }
-	else if (p->prec == MG_PREC_FP32_ID) { e = set_smem_attr<PrecF>(); if (!e) e = occupancy<PrecF>(threads, p->smem, p->kt_t, p->threads_t, p->smem_t, per_sm, per_sm_t); }
-	else { e = set_smem_attr<PrecX>(); if (!e) e = occupancy<PrecX>(threads, p->smem, p->kt_t, p->threads_t, p->smem_t, per_sm, per_sm_t); }
+	if (p->prec == MG_PREC_FP64_ID) { e = set_smem_attr<PrecD>(); if (!e) e = occupancy<PrecD>(threads, p->smem, p->kt_t, p->threads_t, p->nc_t, p->smem_t, per_sm, per_sm_t); }
+	else if (p->prec == MG_PREC_FP32_ID) { e = set_smem_attr<PrecF>(); if (!e) e = occupancy<PrecF>(threads, p->smem, p->kt_t, p->threads_t, p->nc_t, p->smem_t, per_sm, per_sm_t); }
+	else { e = set_smem_attr<PrecX>(); if (!e) e = occupancy<PrecX>(threads, p->smem, p->kt_t, p->threads_t, p->nc_t, p->smem_t, per_sm, per_sm_t); }
 	if (e) { delete p; return nullptr; }
 	const long opt_cps = mgcu_option(MG_OPT_CTAS_PER_SM_ID);
 	if (opt_cps > 0) per_sm = (int)std::min<long>(per_sm, opt_cps);

@@ -32,7 +32,8 @@ extern "C" {
 #define MG_OPT_CTAS_PER_SM_ID   4
 #define MG_OPT_TARGET_TILE_BITS_ID 5
 #define MG_OPT_TARGET_THREADS_ID   6
-#define MG_NOPTIONS             6
+#define MG_OPT_TARGET_COLUMNS_ID   7
+#define MG_NOPTIONS             7
 
 /* ---- runtime ---- */
 void mg_set_error(const char* fmt, ...);

@@ -22,7 +22,7 @@ DEFAULT_LIB = os.path.join(HERE, "_build", "libmgcu.so")
 
 PREC_FP64, PREC_MIXED, PREC_FP32 = 0, 1, 2
 OPT_TILE_BITS, OPT_THREADS, OPT_CHUNK_COLUMNS, OPT_CTAS_PER_SM = 1, 2, 3, 4
-OPT_TARGET_TILE_BITS, OPT_TARGET_THREADS = 5, 6
+OPT_TARGET_TILE_BITS, OPT_TARGET_THREADS, OPT_TARGET_COLUMNS = 5, 6, 7
 EVAL_TARGET, EVAL_GRADIENT, EVAL_HESSIAN, EVAL_TI = 0, 1, 2, 4
 
 P = C.c_void_p

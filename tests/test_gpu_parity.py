@@ -503,3 +503,34 @@ def test_fswap_relabelling_vs_oracle(lib, oracle, L, prec, paired, tile_bits):
     f_o, dv_o = oracle.brickwall_target_and_gradient(oracle.Target("circuit", L, gates=gates, wires=wires), v, perms, L, col_range=cols)
     sf, sg = max(1.0, abs(f_o)), max(1.0, np.max(np.abs(dv_o)))
     assert abs(f - f_o) < tol * sf and np.max(np.abs(dv - dv_o)) < tol * sg
+
+
+@pytest.mark.parametrize("L,prec,tile_bits,cols", [(12, mgcu.PREC_FP64, 0, (0, 96)), (14, mgcu.PREC_MIXED, 0, (3, 70)),
+                                                   (14, mgcu.PREC_FP64, 12, (5, 7)), (14, mgcu.PREC_FP32, 0, (0, 64)),
+                                                   (12, mgcu.PREC_MIXED, 9, (1, 50))])
+def test_two_columns_per_block_vs_oracle(lib, oracle, L, prec, tile_bits, cols):
+    """the target sweep with two basis columns of equal parity per block (and single
+    columns outside whole groups of four), fermionic swaps and structured gates"""
+    rng = np.random.default_rng(400 + L + tile_bits)
+    g1, w1 = _fswap_circuit(L, 60, rng)
+    g2 = np.concatenate([_structured_gates(30, rng), random_gates(30, rng, unitary=True)])
+    w2 = np.array([rng.choice(L, 2, replace=False) for _ in range(60)], np.int32)
+    gates, wires = np.concatenate([g1, g2]), np.concatenate([w1, w2])
+    v = random_gates(3, rng, unitary=True)
+    perms = brickwall_perms(L, 3, rng)
+    t = lib.target_circuit(gates, wires, L)
+    lib.set_precision(prec)
+    lib.set_option(mgcu.OPT_TILE_BITS, tile_bits)
+    lib.set_option(mgcu.OPT_TARGET_COLUMNS, 2)
+    try:
+        rc, f, dv = lib.brickwall_columns(lib.mg_target_apply, t, v, perms, L, *cols)
+    finally:
+        lib.set_option(mgcu.OPT_TARGET_COLUMNS, 0)
+        lib.set_option(mgcu.OPT_TILE_BITS, 0)
+        lib.set_precision(mgcu.PREC_FP64)
+        lib.target_free(t)
+    assert rc == 0
+    tol = 1e-4 if prec == mgcu.PREC_FP32 else 1e-12
+    f_o, dv_o = oracle.brickwall_target_and_gradient(oracle.Target("circuit", L, gates=gates, wires=wires), v, perms, L, col_range=cols)
+    sf, sg = max(1.0, abs(f_o)), max(1.0, np.max(np.abs(dv_o)))
+    assert abs(f - f_o) < tol * sf and np.max(np.abs(dv - dv_o)) < tol * sg
