@@ -2252,6 +2252,9 @@ struct BatchInst
 	mgcu_target* target;
 	size_t smem_t, pm_off, smem_c;
 	double col_cost;               // relative cost of one column
+	bool big = false;              // enough columns to fill the GPU: its own kernels
+	int grid_t = 0, grid_c = 0;    // standalone grids (big instances)
+	long chunk = 0;                // columns per staged chunk (big instances)
 	long part_off;                 // offsets (doubles) of part_f / part_g in the batch's partials
 	long part_g_off;
 };
@@ -2267,6 +2270,8 @@ struct mgcu_batch
 	long slot_stride = 0, cache_stride = 0;
 	size_t smem = 0;
 	int grid[3] = { 0, 0, 0 }, nitems = 0;
+	DevBuf stage, bsu, bsw, bcache;   // big instances: staged target columns, k_columns slots and caches
+	std::vector<char> host_args;      // the instances' target and columns Args (kernel parameters of big ones)
 	int class_beg[4] = { 0, 0, 0, 0 };   // items of tile classes 4, 8, any quartets per thread
 	long graph_kernels = 0;        // kernel nodes per replay
 	bool use_graph = true;         // false: plain launches (a batch run once)
@@ -2402,15 +2407,48 @@ static int batch_build(mgcu_batch* B, const mgcu_batch_inst* d, int tune)
 		return (Q == 4L * threads) ? 0 : (Q == 8L * threads) ? 1 : 2;
 	};
 
-	// work items: about 16 per block, never more than an instance's columns, largest first
+	// Instances with at least four columns per resident block run the two standalone
+	// kernels (k_target into a staged chunk, then k_columns), which are faster per column
+	// than the fused kernel; the others share the fused persistent launch.
+	size_t stage_bytes = 0, slot_max = 0, cache_max = 0;
+	int grid_c_max = 0;
+	for (int i = 0; i < B->n; i++)
+	{
+		BatchInst& I = B->inst[i];
+		void (*kt_)(Args<P>) = target_kernel<P>(I.kt_t, threads);
+		int pt = 0, pc = 0;
+		MGCU_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&pt, kt_, threads, I.smem_t));
+		MGCU_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&pc, k_columns<P, false>, threads, I.smem_c));
+		I.grid_t = c->nsm * std::max(pt, 1);
+		I.grid_c = c->nsm * std::max(pc, 1);
+		I.big = (1L << I.L) >= 4L * std::max(I.grid_t, I.grid_c);
+		if (!I.big) continue;
+		I.chunk = std::max(1L, std::min(1L << I.L, (long)((8ull << 30) / ((size_t)I.S * sizeof(T)))));
+		stage_bytes = std::max(stage_bytes, sizeof(T) * (size_t)I.S * (size_t)I.chunk);
+		slot_max = std::max(slot_max, (size_t)I.S);
+		if (d[i].want_grad) cache_max = std::max(cache_max, (size_t)I.S * (size_t)I.ngates);
+		grid_c_max = std::max(grid_c_max, I.grid_c);
+	}
+	if (stage_bytes)
+	{
+		int e = B->stage.alloc(stage_bytes);
+		if (!e) e = B->bsu.alloc(sizeof(T) * slot_max * grid_c_max);
+		if (!e) e = B->bsw.alloc(sizeof(T) * slot_max * grid_c_max);
+		if (!e && cache_max) e = B->bcache.alloc(sizeof(T) * cache_max * grid_c_max);
+		if (e) return e;
+	}
+
+	// work items of the other instances: about 16 per block, never more than an
+	// instance's columns, largest first
 	double total = 0;
-	for (int i = 0; i < B->n; i++) total += B->inst[i].col_cost * (double)(1L << B->inst[i].L);
+	for (int i = 0; i < B->n; i++) if (!B->inst[i].big) total += B->inst[i].col_cost * (double)(1L << B->inst[i].L);
 	const double item_cost = total / (16.0 * B->grid[0]);
 	struct HostItem { BatchItem it; double cost; };
 	std::vector<HostItem> all;
 	for (int i = 0; i < B->n; i++)
 	{
 		BatchInst& I = B->inst[i];
+		if (I.big) { I.nslots = I.grid_c; continue; }   // partial rows: one per k_columns block
 		const long N = 1L << I.L;
 		const long per = std::max(1L, std::min(N, (long)(item_cost / I.col_cost)));
 		for (long b0 = 0; b0 < N; b0 += per)
@@ -2484,6 +2522,9 @@ static int batch_build(mgcu_batch* B, const mgcu_batch_inst* d, int tune)
 	}
 	MGCU_TRY(cudaMemcpy(B->args_t.p, at.data(), sizeof(Args<P>) * B->n, cudaMemcpyHostToDevice));
 	MGCU_TRY(cudaMemcpy(B->args_c.p, ac.data(), sizeof(Args<P>) * B->n, cudaMemcpyHostToDevice));
+	B->host_args.resize(sizeof(Args<P>) * 2 * B->n);
+	memcpy(B->host_args.data(), at.data(), sizeof(Args<P>) * B->n);
+	memcpy(B->host_args.data() + sizeof(Args<P>) * B->n, ac.data(), sizeof(Args<P>) * B->n);
 	MGCU_TRY(cudaMemcpy(B->red.p, rd.data(), sizeof(BatchRed) * B->n, cudaMemcpyHostToDevice));
 	return 0;
 }
@@ -2496,6 +2537,29 @@ static int batch_issue(mgcu_batch* B)
 	cudaStream_t st = mgcu_ctx()->stream;
 	MGCU_TRY(cudaMemsetAsync(B->parts.p, 0, B->parts.n, st));
 	MGCU_TRY(cudaMemsetAsync(B->counters.p, 0, B->counters.n, st));
+	const Args<P>* hat = reinterpret_cast<const Args<P>*>(B->host_args.data());
+	const Args<P>* hac = hat + B->n;
+	for (int i = 0; i < B->n; i++)
+	{
+		const BatchInst& I = B->inst[i];
+		if (!I.big) continue;
+		void (*kt_)(Args<P>) = target_kernel<P>(I.kt_t, B->threads);
+		const long N = 1L << I.L;
+		for (long c0 = 0; c0 < N; c0 += I.chunk)
+		{
+			const long c1 = std::min(N, c0 + I.chunk);
+			Args<P> a = hat[i];
+			a.b0 = c0; a.b1 = c1; a.ucols = B->stage.as<T>();
+			kt_<<<(int)std::min<long>(I.grid_t, c1 - c0), B->threads, I.smem_t, st>>>(a);
+			MGCU_LAUNCHED();
+			Args<P> w = hac[i];
+			w.b0 = c0; w.b1 = c1; w.dense = B->stage.as<T>(); w.dense_b0 = c0;
+			w.su = B->bsu.as<T>(); w.sw = B->bsw.as<T>();
+			w.cache = w.want_grad ? B->bcache.as<T>() : nullptr;
+			k_columns<P, false><<<(int)std::min<long>(I.grid_c, c1 - c0), B->threads, I.smem_c, st>>>(w);
+			MGCU_LAUNCHED();
+		}
+	}
 	void (*const kb[3])(const Args<P>*, const Args<P>*, const BatchItem*, int, int*, T*, long, long) = { k_batch<P, 4>, k_batch<P, 8>, k_batch<P, 0> };
 	for (int k = 0; k < 3; k++)
 	{
