@@ -47,7 +47,9 @@ def build(force=False, verbose=False):
     for s in cu:
         o = _obj(s)
         if force or _stale(o, [s, __file__] + hdr):
-            jobs.append(([NVCC] + ARCH + ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC"] + INC
+            # the engine is one large translation unit: let nvcc optimise its kernels in parallel
+            split = ["--split-compile=0"] if os.path.basename(s) == "mgcu_engine.cu" else []
+            jobs.append(([NVCC] + ARCH + ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC"] + split + INC
                          + ["-c", s, "-o", o], s))
     for s in c:
         o = _obj(s)
