@@ -64,6 +64,20 @@ int mg_target_set_resident(void* udata, int enable);
 int mg_target_sweep_gates(void* udata);
 
 /* ---------------------------------------------------------------------------------
+ * Target construction (the reference builds its benchmark targets in Python,
+ * benchmark_hpc/spl_hubbard1d_bench_init.py:24-118, test/rqcopt_matfree/splitting_method.py:
+ * 161-193): the spinful 1-D Fermi-Hubbard model on nsites sites (2 nsites qubits,
+ * interleaved spins, Jordan-Wigner, open chain), H = U sum n_up n_down - J sum hops, as a
+ * Suzuki product formula of even order (2, 4, ...) with nsteps steps over time t, built
+ * from on-site phases, hopping matchgates and fermionic swaps.
+ * mg_hubbard_trotter_circuit writes the gates and wires when capacity suffices and returns
+ * the gate count (< 0 on bad arguments); mg_target_hubbard returns a GPU target of it.
+ * --------------------------------------------------------------------------------- */
+int mg_hubbard_trotter_circuit(int nsites, double J, double U, double t, int nsteps, int order,
+                               struct matchgate gates[], int wires[], int capacity);
+void* mg_target_hubbard(int nsites, double J, double U, double t, int nsteps, int order);
+
+/* ---------------------------------------------------------------------------------
  * Batches: f and the layer gradients of many independent brickwall fits at once, each
  * against its own GPU circuit target (mg_target_circuit / mg_target_brickwall), any
  * even qubit count and depth.  One persistent launch per phase covers every instance:

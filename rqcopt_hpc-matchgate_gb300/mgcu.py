@@ -127,6 +127,9 @@ class MatchgateLib:
             L.mg_batch_time_ms.argtypes = [P, C.c_int, C.c_int]
             L.mg_batch_time_ms.restype = C.c_double
             L.mg_batch_free.argtypes = [P]
+            L.mg_hubbard_trotter_circuit.argtypes = [C.c_int, C.c_double, C.c_double, C.c_double, C.c_int, C.c_int, P, P, C.c_int]
+            L.mg_target_hubbard.restype = P
+            L.mg_target_hubbard.argtypes = [C.c_int, C.c_double, C.c_double, C.c_double, C.c_int, C.c_int]
             L.mg_server_create.restype = P
             L.mg_server_create.argtypes = [C.c_size_t, C.c_int]
             L.mg_server_submit.restype = C.c_long
@@ -226,6 +229,17 @@ class MatchgateLib:
     def batch_free(self, batch):
         self.lib.mg_batch_free(P(batch["ptr"]))
         batch["ptr"] = None
+
+    # ------------------------------------------------------------------ target construction
+    def hubbard_trotter_circuit(self, nsites, J, U, t, nsteps, order=2):
+        """(gates [n, 8], wires [n, 2]) of the Suzuki circuit built by the library"""
+        n = self.lib.mg_hubbard_trotter_circuit(nsites, J, U, t, nsteps, order, None, None, 0)
+        if n < 0:
+            raise RuntimeError(self.last_error())
+        g = np.zeros((n, 8), cd); w = np.zeros((n, 2), np.int32)
+        n2 = self.lib.mg_hubbard_trotter_circuit(nsites, J, U, t, nsteps, order, _p(g), _p(w), n)
+        assert n2 == n
+        return g, w
 
     # ------------------------------------------------------------------ request server
     def server_create(self, budget_bytes, max_batch=256):

@@ -534,3 +534,21 @@ def test_two_columns_per_block_vs_oracle(lib, oracle, L, prec, tile_bits, cols):
     f_o, dv_o = oracle.brickwall_target_and_gradient(oracle.Target("circuit", L, gates=gates, wires=wires), v, perms, L, col_range=cols)
     sf, sg = max(1.0, abs(f_o)), max(1.0, np.max(np.abs(dv_o)))
     assert abs(f - f_o) < tol * sf and np.max(np.abs(dv - dv_o)) < tol * sg
+
+
+def test_hubbard_target_constructor_vs_oracle(lib, oracle):
+    """mg_target_hubbard (fourth-order Suzuki circuit built by the library) as a GPU target"""
+    L = 8
+    g, w = lib.hubbard_trotter_circuit(L // 2, 1.0, 4.0, 0.25, 3, 4)
+    t = lib.lib.mg_target_hubbard(L // 2, 1.0, 4.0, 0.25, 3, 4)
+    assert t
+    rng = np.random.default_rng(17)
+    v = random_gates(3, rng, unitary=True)
+    perms = brickwall_perms(L, 3, rng)
+    try:
+        rc, f, dv = lib.brickwall_target_and_gradient(lib.mg_target_apply, t, v, perms, L)
+    finally:
+        lib.target_free(t)
+    assert rc == 0
+    f_o, dv_o = oracle.brickwall_target_and_gradient(oracle.Target("circuit", L, gates=g, wires=w), v, perms, L)
+    assert abs(f - f_o) < 1e-12 * max(1, abs(f_o)) and udist(dv, dv_o) < 1e-12 * max(1, np.max(np.abs(dv_o)))
