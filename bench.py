@@ -274,6 +274,28 @@ def run_gb300(a):
     rel_f = abs(fx - f64) / abs(f64)
     rel_g = float(np.linalg.norm(dvx - dv64) / np.linalg.norm(dv64))
 
+    # optimiser steady state: the target's columns kept resident on the GPU after one sweep
+    # (reported beside the headline, which sweeps the target in every evaluation)
+    resident = None
+    if world == 1:
+        lib.set_precision(prec)
+        lib.target_set_resident(target, True)
+        plan_r = lib.plan_brickwall(lib.mg_target_apply, target, v, perms, L, mgcu.EVAL_GRADIENT)
+        t0 = time.perf_counter()
+        assert lib.lib.mg_plan_run(mgcu.P(plan_r)) == 0, lib.last_error()   # fills the resident columns
+        lib.plan_results(plan_r, nl, grad=True)                              # (waits for the GPU)
+        fill_s = time.perf_counter() - t0
+        ms_r = lib.lib.mg_plan_time_ms(mgcu.P(plan_r), a.steps, 1)
+        f_r, _, _, gvec_r, _ = lib.plan_results(plan_r, nl, grad=True, proj=True)
+        lib.lib.mg_plan_free(mgcu.P(plan_r))
+        lib.target_set_resident(target, False)
+        resident = {"value": a.steps / (ms_r / 1e3), "unit": UNIT, "first_evaluation_s": fill_s,
+                    "device_bytes": (1 << L) * (1 << (L - 1)) * (16 if prec != mgcu.PREC_FP32 else 8),
+                    "same_result": bool(abs(f_r - f_dev) <= 1e-12 * abs(f_dev)),
+                    "note": "the target's -conj(U e_b) columns stay on the GPU after the first evaluation "
+                            "(mg_target_set_resident); later evaluations with new fitted gates run only the "
+                            "fitted circuit; not the headline, which sweeps the target every evaluation"}
+
     flops = alg_flops(L, gu, gw, ncols)
     achieved_step = flops / (ms_per_step / 1e3) / 1e12
     # dominant kernel: the target sweep (k_target), timed by CUDA events around each launch
@@ -317,6 +339,7 @@ def run_gb300(a):
         "accuracy": {"rel_err_f_vs_fp64": rel_f, "rel_err_grad_vs_fp64": rel_g, "columns": c,
                      "f": [float(np.real(f_dev)), float(np.imag(f_dev))]},
         "serving": None,
+        "resident_target": resident,
     }
     if rank == 0 and world == 1 and not a.no_cpu:
         cv, cores, cc, cs = cpu_baseline(g, w, v, perms, L, a.cpu_seconds)

@@ -304,6 +304,9 @@ class MatchgateLib:
             raise RuntimeError("mg_target_dense failed: " + self.last_error())
         return h
 
+    def target_set_resident(self, h, enable=True):
+        return self.lib.mg_target_set_resident(P(h), int(bool(enable)))
+
     def target_free(self, h):
         self.lib.mg_target_free(h)
 

@@ -552,3 +552,30 @@ def test_hubbard_target_constructor_vs_oracle(lib, oracle):
     assert rc == 0
     f_o, dv_o = oracle.brickwall_target_and_gradient(oracle.Target("circuit", L, gates=g, wires=w), v, perms, L)
     assert abs(f - f_o) < 1e-12 * max(1, abs(f_o)) and udist(dv, dv_o) < 1e-12 * max(1, np.max(np.abs(dv_o)))
+
+
+@pytest.mark.parametrize("prec", [mgcu.PREC_FP64, mgcu.PREC_MIXED])
+def test_resident_target_columns(lib, oracle, prec):
+    """target columns kept resident on the GPU after the first evaluation: later
+    evaluations with other fitted gates give the same results as sweeping the target"""
+    L = 12
+    rng = np.random.default_rng(55)
+    gates, wires = _fswap_circuit(L, 80, rng)
+    perms = brickwall_perms(L, 3, rng)
+    vs = [random_gates(3, rng, unitary=True) for _ in range(3)]
+    t = lib.target_circuit(gates, wires, L)
+    lib.set_precision(prec)
+    try:
+        plain = [lib.brickwall_target_and_gradient(lib.mg_target_apply, t, v, perms, L) for v in vs]
+        assert lib.target_set_resident(t, True) == 0
+        res = [lib.brickwall_target_and_gradient(lib.mg_target_apply, t, v, perms, L) for v in vs]
+        assert lib.target_set_resident(t, False) == 0
+    finally:
+        lib.set_precision(mgcu.PREC_FP64)
+        lib.target_free(t)
+    ot = oracle.Target("circuit", L, gates=gates, wires=wires)
+    for (rc, f, dv), (rc2, f2, dv2), v in zip(plain, res, vs):
+        assert rc == 0 and rc2 == 0
+        assert abs(f - f2) < 1e-12 * max(1, abs(f)) and np.max(np.abs(dv - dv2)) < 1e-12 * max(1, np.max(np.abs(dv)))
+        f_o, dv_o = oracle.brickwall_target_and_gradient(ot, v, perms, L)
+        assert abs(f2 - f_o) < 1e-12 * max(1, abs(f_o)) and udist(dv2, dv_o) < 1e-12 * max(1, np.max(np.abs(dv_o)))
