@@ -64,6 +64,19 @@ int mg_target_set_resident(void* udata, int enable);
 int mg_target_sweep_gates(void* udata);
 
 /* ---------------------------------------------------------------------------------
+ * Native trust-region fit (the loop of riemannian_trust_region_optimize_hmat,
+ * src/trust_region.c:235-306, driven as optimize_matchgate_brickwall_circuit_hmat,
+ * src/mg_brickwall_opt.c:99-122, on device-resident evaluation plans of a GPU target).
+ * With refine_gnorm > 0 the evaluations run in float-float until the Riemannian gradient
+ * norm falls below refine_gnorm, then in complex128 to the end; refine_gnorm <= 0: complex128
+ * throughout.  f_iter [niter+1] gets Re f of every iterate (the last one at vlist_out),
+ * prec_iter [niter+1] (may be NULL) the precision each was evaluated in.
+ * --------------------------------------------------------------------------------- */
+int mg_optimize_brickwall(void* target, const struct matchgate vlist0[], int nlayers, int nqubits, const int* perms[],
+                          const struct rtr_params* params, int niter, double refine_gnorm, double f_iter[], int prec_iter[],
+                          struct matchgate vlist_out[]);
+
+/* ---------------------------------------------------------------------------------
  * Target construction (the reference builds its benchmark targets in Python,
  * benchmark_hpc/spl_hubbard1d_bench_init.py:24-118, test/rqcopt_matfree/splitting_method.py:
  * 161-193): the spinful 1-D Fermi-Hubbard model on nsites sites (2 nsites qubits,

@@ -1,0 +1,132 @@
+/*
+ * Native trust-region fit of a brickwall circuit against a GPU target, with the
+ * evaluations on device-resident plans and a switch from float-float to complex128
+ * evaluations near convergence.
+ *
+ * The loop is the reference's riemannian_trust_region_optimize_hmat
+ * (src/trust_region.c:235-306) driven as optimize_matchgate_brickwall_circuit_hmat drives it
+ * (src/mg_brickwall_opt.c:99-122): target Re f, Riemannian gradient and Hessian
+ * (src/matchgate_target.c:877-973), Steihaug tCG, retraction per layer, the rho test
+ * (rho < 1/4 shrinks the radius by 4, rho > 3/4 on the boundary doubles it up to maxradius,
+ * the step is taken when rho > rho_trust).
+ */
+#include <complex.h>
+#include <math.h>
+#include <stdlib.h>
+#include <string.h>
+
+#include "matchgate_target.h"
+#include "trust_region.h"
+#include "mg_gb300.h"
+#include "../mg_internal.h"
+
+typedef struct { mg_plan* h; mg_plan* f; int prec; } plans_t;
+
+static void plans_free(plans_t* p)
+{
+	if (p->h) mg_plan_free(p->h);
+	if (p->f) mg_plan_free(p->f);
+	p->h = p->f = NULL;
+}
+
+static int plans_make(plans_t* p, void* target, const struct matchgate* v, int nl, int L, const int* perms[], int prec)
+{
+	plans_free(p);
+	const int old = mg_get_precision();
+	mg_set_precision(prec);
+	p->h = mg_plan_brickwall(mg_target_apply, target, v, nl, L, perms, MG_EVAL_HESSIAN);
+	p->f = p->h ? mg_plan_brickwall(mg_target_apply, target, v, nl, L, perms, MG_EVAL_TARGET) : NULL;
+	mg_set_precision(old);
+	p->prec = prec;
+	return (p->h && p->f) ? 0 : MG_ERR_DEVICE;
+}
+
+static int eval_hess(plans_t* p, const struct matchgate* v, double* f, double* grad, double* H)
+{
+	int rc = mg_plan_set_gates(p->h, v);
+	if (!rc) rc = mg_plan_run(p->h);
+	numeric fc = 0;
+	if (!rc) rc = mg_plan_results(p->h, &fc, NULL, NULL, grad, H);
+	if (!rc) *f = creal(fc);
+	return rc;
+}
+
+static int eval_f(plans_t* p, const struct matchgate* v, double* f)
+{
+	int rc = mg_plan_set_gates(p->f, v);
+	if (!rc) rc = mg_plan_run(p->f);
+	numeric fc = 0;
+	if (!rc) rc = mg_plan_results(p->f, &fc, NULL, NULL, NULL, NULL);
+	if (!rc) *f = creal(fc);
+	return rc;
+}
+
+int mg_optimize_brickwall(void* target, const struct matchgate vlist0[], int nlayers, int nqubits, const int* perms[],
+	const struct rtr_params* params, int niter, double refine_gnorm, double f_iter[], int prec_iter[],
+	struct matchgate vlist_out[])
+{
+	if (!target || !vlist0 || nlayers < 1 || !perms || !params || niter < 0 || !f_iter || !vlist_out)
+	{
+		mg_set_error("mg_optimize_brickwall: bad arguments");
+		return MG_ERR_ARG;
+	}
+	const int n = 8 * nlayers;
+	struct matchgate* x = malloc(sizeof(struct matchgate) * nlayers);
+	struct matchgate* xn = malloc(sizeof(struct matchgate) * nlayers);
+	double* grad = malloc(sizeof(double) * n);
+	double* H = malloc(sizeof(double) * (size_t)n * n);
+	double* eta = malloc(sizeof(double) * n);
+	if (!x || !xn || !grad || !H || !eta) { free(x); free(xn); free(grad); free(H); free(eta); return MG_ERR_ALLOC; }
+	memcpy(x, vlist0, sizeof(struct matchgate) * nlayers);
+	plans_t pl = { 0 };
+	int prec = refine_gnorm > 0 ? MG_PREC_MIXED : MG_PREC_FP64;
+	int rc = plans_make(&pl, target, x, nlayers, nqubits, perms, prec);
+	double radius = params->radius_init;
+	for (int k = 0; k < niter && !rc; k++)
+	{
+		double fx;
+		rc = eval_hess(&pl, x, &fx, grad, H);
+		if (rc) break;
+		if (prec == MG_PREC_MIXED)
+		{
+			double g2 = 0;
+			for (int i = 0; i < n; i++) g2 += grad[i] * grad[i];
+			if (sqrt(g2) < refine_gnorm)
+			{
+				/* near convergence: complex128 from here on, this iterate re-evaluated */
+				prec = MG_PREC_FP64;
+				rc = plans_make(&pl, target, x, nlayers, nqubits, perms, prec);
+				if (!rc) rc = eval_hess(&pl, x, &fx, grad, H);
+				if (rc) break;
+			}
+		}
+		f_iter[k] = fx;
+		if (prec_iter) prec_iter[k] = prec;
+		const bool on_boundary = truncated_cg_hmat(grad, H, n, radius, &params->tcg_params, eta);
+		for (int l = 0; l < nlayers; l++) retract_matchgate(&x[l], eta + 8 * l, &xn[l]);
+		double fn;
+		rc = eval_f(&pl, xn, &fn);
+		if (rc) break;
+		double ge = 0, eHe = 0;
+		for (int i = 0; i < n; i++)
+		{
+			double s = 0;
+			for (int j = 0; j < n; j++) s += H[(size_t)i * n + j] * eta[j];
+			ge += grad[i] * eta[i];
+			eHe += eta[i] * s;
+		}
+		const double rho = (fn - fx) / (ge + 0.5 * eHe);
+		if (rho < 0.25) radius *= 0.25;
+		else if (rho > 0.75 && on_boundary) radius = fmin(2 * radius, params->maxradius);
+		if (rho > params->rho_trust) memcpy(x, xn, sizeof(struct matchgate) * nlayers);
+	}
+	if (!rc)
+	{
+		rc = eval_f(&pl, x, &f_iter[niter]);
+		if (prec_iter) prec_iter[niter] = prec;
+		memcpy(vlist_out, x, sizeof(struct matchgate) * nlayers);
+	}
+	plans_free(&pl);
+	free(x); free(xn); free(grad); free(H); free(eta);
+	return rc;
+}

@@ -130,6 +130,7 @@ class MatchgateLib:
             L.mg_hubbard_trotter_circuit.argtypes = [C.c_int, C.c_double, C.c_double, C.c_double, C.c_int, C.c_int, P, P, C.c_int]
             L.mg_target_hubbard.restype = P
             L.mg_target_hubbard.argtypes = [C.c_int, C.c_double, C.c_double, C.c_double, C.c_int, C.c_int]
+            L.mg_optimize_brickwall.argtypes = [P, P, C.c_int, C.c_int, P, C.POINTER(RtrParams), C.c_int, C.c_double, P, P, P]
             L.mg_server_create.restype = P
             L.mg_server_create.argtypes = [C.c_size_t, C.c_int]
             L.mg_server_submit.restype = C.c_long
@@ -229,6 +230,21 @@ class MatchgateLib:
     def batch_free(self, batch):
         self.lib.mg_batch_free(P(batch["ptr"]))
         batch["ptr"] = None
+
+    def optimize_native(self, target, vlist0, perms, L, niter, refine_gnorm=0.0, tcg_maxiter=None,
+                        rho_trust=0.125, radius_init=0.01, maxradius=0.1):
+        """mg_optimize_brickwall: (f_iter [niter+1], prec_iter [niter+1], final gates)"""
+        v0 = gates_arr(vlist0); nl = len(v0)
+        pp, rows = _perm_ptrs(perms, L)
+        prm = RtrParams()
+        prm.tcg_params = TcgParams(tcg_maxiter if tcg_maxiter is not None else 2 * 16 * nl, 1e-8, 1e-6)
+        prm.rho_trust, prm.radius_init, prm.maxradius = rho_trust, radius_init, maxradius
+        f_iter = np.zeros(niter + 1); prec = np.zeros(niter + 1, np.int32); xf = np.zeros((nl, 8), cd)
+        rc = self.lib.mg_optimize_brickwall(P(target), _p(v0), nl, L, C.cast(pp, P), C.byref(prm), niter, refine_gnorm,
+                                            _p(f_iter), _p(prec), _p(xf))
+        if rc != 0:
+            raise RuntimeError(self.last_error())
+        return f_iter, prec, xf
 
     # ------------------------------------------------------------------ target construction
     def hubbard_trotter_circuit(self, nsites, J, U, t, nsteps, order=2):

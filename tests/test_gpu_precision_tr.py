@@ -96,3 +96,28 @@ def test_trust_region_matches_oracle(lib, oracle):
     assert np.max(np.abs(f_g - f_o)) < 1e-8
     assert udist(v_g, v_o) < 1e-8
     assert f_g[-1] < f_g[0]
+
+
+def test_native_trust_region_and_refinement(lib, oracle):
+    """mg_optimize_brickwall: complex128 throughout matches the oracle's 10 iterations;
+    float-float first with the switch to complex128 near convergence reaches the same
+    iterates to 1e-9"""
+    rng = np.random.default_rng(1)
+    L, nl, ul = 8, 4, 8
+    perms = brickwall_perms(L, nl)
+    uperms = brickwall_perms(L, ul)
+    ulist = random_gates(ul, rng, unitary=True)
+    v0 = random_gates(nl, rng, unitary=True)
+    niter = 10
+    t = lib.target_brickwall(ulist, uperms, L)
+    try:
+        f64, p64, v64 = lib.optimize_native(t, v0, perms, L, niter)
+        fmx, pmx, vmx = lib.optimize_native(t, v0, perms, L, niter, refine_gnorm=9.0)   # |grad| 12.9 -> 6.6
+    finally:
+        lib.set_precision(mgcu.PREC_FP64)
+        lib.target_free(t)
+    f_o, fc_o, v_o = oracle.rtr_brickwall(oracle.Target("brickwall", L, ulist=ulist, uperms=uperms), v0, perms, L, niter)
+    assert np.all(p64 == mgcu.PREC_FP64)
+    assert np.max(np.abs(f64 - f_o)) < 1e-8 and udist(v64, v_o) < 1e-8
+    assert pmx[0] == mgcu.PREC_MIXED and pmx[-1] == mgcu.PREC_FP64
+    assert np.max(np.abs(fmx - f_o)) < 1e-9 * np.max(np.abs(f_o)) and udist(vmx, v_o) < 1e-8
