@@ -730,12 +730,21 @@ __device__ __forceinline__ void tgt_gate(char* tb, unsigned td, const TGate& r, 
 	const unsigned p0 = (unsigned)(__popc(b0) + tpar) & 1u;
 	const unsigned d1 = r.h.z, d2 = r.h.w, d4 = r.d4;
 	unsigned x[QPT];
-#pragma unroll
-	for (int k = 0; k < QPT; k++)
+	if (SCX == 0)
 	{
-		const unsigned dk = ((k & 1) ? d1 : 0u) ^ ((k & 2) ? d2 : 0u) ^ ((k & 4) ? d4 : 0u);
-		const unsigned pk = p0 ^ (((k & 1) ? dpar : 0u) & 1u) ^ (((k & 2) ? (dpar >> 1) : 0u) & 1u) ^ (((k & 4) ? (dpar >> 2) : 0u) & 1u);
-		x[k] = sb0 ^ dk ^ (pk ? SCX : 0u);
+		// gates on two compact wires: the quartets' x slots are plain offsets
+#pragma unroll
+		for (int k = 0; k < QPT; k++) x[k] = sb0 ^ ((k & 1) ? d1 : 0u) ^ ((k & 2) ? d2 : 0u) ^ ((k & 4) ? d4 : 0u);
+	}
+	else
+	{
+#pragma unroll
+		for (int k = 0; k < QPT; k++)
+		{
+			const unsigned dk = ((k & 1) ? d1 : 0u) ^ ((k & 2) ? d2 : 0u) ^ ((k & 4) ? d4 : 0u);
+			const unsigned pk = p0 ^ (((k & 1) ? dpar : 0u) & 1u) ^ (((k & 2) ? (dpar >> 1) : 0u) & 1u) ^ (((k & 4) ? (dpar >> 2) : 0u) & 1u);
+			x[k] = sb0 ^ dk ^ (pk ? SCX : 0u);
+		}
 	}
 	const int kw = r.h.x >> 13;
 	const typename P::T* m = mats + (size_t)r.h.y * 8;
