@@ -343,9 +343,14 @@ template <> struct Red<PrecX> : Red<PrecF> {};
 
 // Reduce 8 complex accumulators over the block and add w * (sum) to dst[0..15]
 // (re, im interleaved).  Warp level: a reduce-scatter over 16 reals (16 adds per
-// lane instead of 80); block level: fixed-order FP64 sums over warps.
+// lane instead of 80); block level: fixed-order FP64 sums over warps.  One barrier per
+// call: successive calls (counted in nred, uniform over the block) alternate between
+// the two halves of red, and the warp that sums the partials rotates, so the sums and
+// the global read-modify-write of dst overlap the caller's next gate.  The barrier also
+// orders the caller's tile writes before the next gate's reads.  red holds
+// 2 * (blockDim.x / 32) * 16 doubles.
 template <class P>
-__device__ void block_reduce8(const typename P::Acc (&a)[8], double* red, double* dst, double w)
+__device__ void block_reduce8(const typename P::Acc (&a)[8], double* red, double* dst, double w, int& nred)
 {
 	typedef Red<P> RD;
 	typename RD::R v[16];
@@ -384,17 +389,21 @@ __device__ void block_reduce8(const typename P::Acc (&a)[8], double* red, double
 	}
 	RD::add(v[0], RD::shfl(v[0], 1));
 	const int idx = ((lane >> 4) & 1) * 8 + ((lane >> 3) & 1) * 4 + ((lane >> 2) & 1) * 2 + ((lane >> 1) & 1);
-	if ((lane & 1) == 0) red[warp * 16 + idx] = RD::to_d(v[0]);
+	const int nw = blockDim.x >> 5;
+	double* rh = red + (nred & 1) * nw * 16;
+	if ((lane & 1) == 0) rh[warp * 16 + idx] = RD::to_d(v[0]);
 	__syncthreads();
-	if (threadIdx.x < 16)
+	if (warp == (nred >> 1) % nw && lane < 16)
 	{
 		double s = 0;
-		const int nw = blockDim.x >> 5;
-		for (int k = 0; k < nw; k++) s += red[k * 16 + threadIdx.x];
-		dst[threadIdx.x] += w * s;
+		for (int k = 0; k < nw; k++) s += rh[k * 16 + lane];
+		dst[lane] += w * s;
 	}
-	__syncthreads();
+	nred++;
 }
+
+// reduction scratch of a block of `threads` threads (block_reduce8's two halves)
+constexpr size_t red_bytes(int threads) { return (size_t)2 * (threads / 32) * 16 * sizeof(double); }
 
 template <class P>
 __device__ void block_reduce1(const typename P::Acc& a, double* red, double* dst)
@@ -1042,6 +1051,7 @@ __device__ __forceinline__ void w_column(const Args<P>& a, long b, const typenam
 		if (!a.want_grad) return;
 
 		// W backward: tile holds the derivative after the gate
+		int nred = 0;
 		for (int p = a.W.npass - 1; p >= 0; p--)
 		{
 			const PassRec& pr = a.W.pass[p];
@@ -1118,7 +1128,7 @@ __device__ __forceinline__ void w_column(const Args<P>& a, long b, const typenam
 						tile[ey] = P::madd2(G.c0, dy, G.c2, dz);
 						tile[ez] = P::madd2(G.c1, dy, G.c3, dz);
 					}
-					block_reduce8<P>(acc, s.red, a.part_g + ((size_t)prow * a.ngates + r.g) * 16, 1.0);
+					block_reduce8<P>(acc, s.red, a.part_g + ((size_t)prow * a.ngates + r.g) * 16, 1.0, nred);
 				}
 				if (p > 0) tile_store<P>(tile, kt, s, nlb, su, false);
 				__syncthreads();
@@ -1198,6 +1208,7 @@ __global__ void __launch_bounds__(256) k_hessian(Args<P> a, long nitems)
 	const long S = a.S;
 	T* sh = a.sh + (size_t)blockIdx.x * S;
 	double* parth = a.part_h + (size_t)blockIdx.x * a.mdim * a.mdim * 2;
+	int nred = 0;
 
 	for (long it = blockIdx.x; it < nitems; it += gridDim.x)
 	{
@@ -1282,7 +1293,7 @@ __global__ void __launch_bounds__(256) k_hessian(Args<P> a, long nitems)
 							tile[ez] = P::madd2(G.c2, vy, G.c3, vz);
 						}
 					}
-					block_reduce8<P>(acc, s.red, hrow + (size_t)a.block[r.g] * 16, wrow[r.g]);
+					block_reduce8<P>(acc, s.red, hrow + (size_t)a.block[r.g] * 16, wrow[r.g], nred);
 				}
 				if (pp < a.W.npass - 1) tile_store<P>(tile, kt, s, nlb, sh, false);
 				__syncthreads();
@@ -1959,7 +1970,7 @@ extern "C" mgcu_plan* mgcu_plan_create(const mgcu_plan_desc* d)
 	if (opt_thr > 0) threads = (int)std::max(32L, std::min(256L, (opt_thr / 32) * 32));
 	p->threads = threads;
 	// tile, deposit tables, reduction scratch
-	p->smem = ((size_t)1 << p->kt) * p->tsize + 2 * 128 * sizeof(unsigned) + (size_t)(threads / 32) * 16 * sizeof(double);
+	p->smem = ((size_t)1 << p->kt) * p->tsize + 2 * 128 * sizeof(unsigned) + red_bytes(threads);
 
 	schedule(p->L, p->kt, p->wires.data(), d->ngates, false, p->ws);
 
@@ -2386,7 +2397,7 @@ static int batch_build(mgcu_batch* B, const mgcu_batch_inst* d, int tune)
 		if (e) return e;
 		I.npass_t = (int)I.tp.sched.pass.size();
 		I.smem_t = target_smem<P>(I.kt_t, threads, sizeof(T), I.pm_off);
-		I.smem_c = ((size_t)1 << I.kt_c) * sizeof(T) + 2 * 128 * sizeof(unsigned) + (size_t)(threads / 32) * 16 * sizeof(double);
+		I.smem_c = ((size_t)1 << I.kt_c) * sizeof(T) + 2 * 128 * sizeof(unsigned) + red_bytes(threads);
 		schedule(I.L, I.kt_c, D.wires, D.ngates, false, I.ws);
 		e = upload_sched(I.ws, I.d_pass, I.d_gate);
 		if (!e) e = I.d_mats.alloc(sizeof(T) * 8 * std::max(D.ngates, 1));
@@ -2835,7 +2846,7 @@ extern "C" int mg_noalloc_brickwall_target_and_gradient(const void* ugates, int 
 	const int grid = (int)std::min<long>(NA_BLOCKS, ncols);
 	const int kt = L - 1;
 	const int threads = std::max(32, std::min(256, 1 << (kt - 2)));
-	const size_t smem = ((size_t)1 << kt) * sizeof(double2) + 2 * 128 * sizeof(unsigned) + (size_t)(threads / 32) * 16 * sizeof(double);
+	const size_t smem = ((size_t)1 << kt) * sizeof(double2) + 2 * 128 * sizeof(unsigned) + red_bytes(threads);
 #define NA_TRY(x) do { cudaError_t _e = (x); if (_e != cudaSuccess) { rc = mgcu_check(_e, #x, __FILE__, __LINE__); goto done; } } while (0)
 	NA_TRY(cudaMemcpyAsync(base + NA_WMAT, na_wmat_h, sizeof(double2) * 8 * ng, cudaMemcpyHostToDevice, st));
 	if (ungates) NA_TRY(cudaMemcpyAsync(base + NA_UMAT, na_umat_h, sizeof(double2) * 8 * ungates, cudaMemcpyHostToDevice, st));
