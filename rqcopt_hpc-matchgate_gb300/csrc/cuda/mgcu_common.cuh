@@ -142,6 +142,8 @@ struct PrecD
 		s.re = fma(d.x, x.x, fma(-d.y, x.y, s.re));
 		s.im = fma(d.x, x.y, fma(d.y, x.x, s.im));
 	}
+	// short sums (a few quartets per thread, then a block reduction): same as acc_mul_add
+	__device__ static void acc_mul_add_short(Acc& s, T d, T x) { acc_mul_add(s, d, x); }
 	__device__ static void acc_add(Acc& s, const Acc& o) { s.re += o.re; s.im += o.im; }
 	__device__ static Acc shfl_xor(const Acc& a, int m)
 	{
@@ -191,6 +193,7 @@ struct PrecF
 		two_sum(s.rh, pr, t, e); s.rh = t; s.rl += e;
 		two_sum(s.ih, pi, t, e); s.ih = t; s.il += e;
 	}
+	__device__ static void acc_mul_add_short(Acc& s, T d, T x) { acc_mul_add(s, d, x); }
 	__device__ static void acc_add(Acc& s, const Acc& o) { ff_add(s.rh, s.rl, o.rh, o.rl); ff_add(s.ih, s.il, o.ih, o.il); }
 	__device__ static Acc shfl_xor(const Acc& a, int m)
 	{
@@ -275,6 +278,17 @@ struct PrecX
 		float a, b;
 		fast_two_sum(s.rh, s.rl, a, b); s.rh = a; s.rl = b;
 		fast_two_sum(s.ih, s.il, a, b); s.ih = a; s.il = b;
+	}
+	// the same without renormalising, for sums of at most a few hundred products that are
+	// renormalised when reduced (ff_add): hi is the rounded sum of the exact hi products,
+	// lo collects every rounding error, and |lo| <= n ulp(hi) keeps hi + lo within
+	// n 2^-48 of the exact sum relative to hi
+	__device__ static void acc_mul_add_short(Acc& s, T d, T x)
+	{
+		ff_acc_prod(s.rh, s.rl, d.x, d.z, x.x, x.z);
+		ff_acc_prod(s.rh, s.rl, -d.y, -d.w, x.y, x.w);
+		ff_acc_prod(s.ih, s.il, d.x, d.z, x.y, x.w);
+		ff_acc_prod(s.ih, s.il, d.y, d.w, x.x, x.z);
 	}
 	__device__ static void acc_add(Acc& s, const Acc& o) { PrecF::acc_add(s, o); }
 	__device__ static Acc shfl_xor(const Acc& a, int m) { return PrecF::shfl_xor(a, m); }

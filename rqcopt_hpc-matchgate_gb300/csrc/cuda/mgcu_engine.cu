@@ -516,15 +516,16 @@ __device__ __forceinline__ void gate_forward_kinds(typename P::T* tile, const Ga
 }
 
 // contraction of the derivative d (state after the gate, read from dsrc) with the
-// state before the gate x: acc[e] += d_r x_s for the 8 block entries
+// state before the gate x: acc[e] += d_r x_s for the 8 block entries (a thread's
+// quartets of one gate and tile, block-reduced right after)
 template <class P>
 __device__ __forceinline__ void contract_quartet(typename P::Acc (&acc)[8], typename P::T dx, typename P::T dw, typename P::T dy, typename P::T dz,
 	typename P::T x, typename P::T w, typename P::T y, typename P::T z)
 {
-	P::acc_mul_add(acc[0], dy, y); P::acc_mul_add(acc[1], dy, z);
-	P::acc_mul_add(acc[2], dz, y); P::acc_mul_add(acc[3], dz, z);
-	P::acc_mul_add(acc[4], dx, x); P::acc_mul_add(acc[5], dx, w);
-	P::acc_mul_add(acc[6], dw, x); P::acc_mul_add(acc[7], dw, w);
+	P::acc_mul_add_short(acc[0], dy, y); P::acc_mul_add_short(acc[1], dy, z);
+	P::acc_mul_add_short(acc[2], dz, y); P::acc_mul_add_short(acc[3], dz, z);
+	P::acc_mul_add_short(acc[4], dx, x); P::acc_mul_add_short(acc[5], dx, w);
+	P::acc_mul_add_short(acc[6], dw, x); P::acc_mul_add_short(acc[7], dw, w);
 }
 
 // ---- tile transfers ----
@@ -1195,10 +1196,14 @@ __global__ void __launch_bounds__(256, 2) k_batch(const Args<P>* __restrict__ ar
 // ------------------------------------------------------------------------------------
 // stage B: Hessian items (column, placement, entry): the placeholder state of one
 // gate entry pushed through all later gates, contracted at each with the cached
-// derivative (reference src/matchgate_brickwall.c:177-231)
+// derivative (reference src/matchgate_brickwall.c:177-231).  Consecutive gates of a
+// pass with the same block and weight (a brickwall layer) share one block reduction:
+// the thread accumulators carry over, up to HESS_MERGE quartets per thread.
 // ------------------------------------------------------------------------------------
+constexpr int HESS_MERGE = 64;
+
 template <class P>
-__global__ void __launch_bounds__(256) k_hessian(Args<P> a, long nitems)
+__global__ void __launch_bounds__(256, 2) k_hessian(Args<P> a, long nitems)
 {
 	typedef typename P::T T;
 	extern __shared__ __align__(16) char smem_raw[];
@@ -1209,6 +1214,11 @@ __global__ void __launch_bounds__(256) k_hessian(Args<P> a, long nitems)
 	T* sh = a.sh + (size_t)blockIdx.x * S;
 	double* parth = a.part_h + (size_t)blockIdx.x * a.mdim * a.mdim * 2;
 	int nred = 0;
+	const int qpt = (Q + (int)blockDim.x - 1) / (int)blockDim.x;
+	typename P::Acc acc[8];
+#pragma unroll
+	for (int e = 0; e < 8; e++) acc[e] = P::acc_zero();
+	int merged = 0;
 
 	for (long it = blockIdx.x; it < nitems; it += gridDim.x)
 	{
@@ -1276,9 +1286,17 @@ __global__ void __launch_bounds__(256) k_hessian(Args<P> a, long nitems)
 					const Gate8<T> G = load_gate(a.wm, r.g);
 					const T* dg = dcache + (size_t)r.g * S + ((size_t)tau << kt);   // tile order
 					const bool apply = (r.g != a.ngates - 1);
-					typename P::Acc acc[8];
-#pragma unroll
-					for (int e = 0; e < 8; e++) acc[e] = P::acc_zero();
+					const int blk = a.block[r.g];
+					const double wg = wrow[r.g];
+					// the next gate of the pass (a later one: passes keep the sequential
+					// order) continues this reduction when it has the same block and weight
+					merged += qpt;
+					bool flush = true;
+					if (gi + 1 < pr.gend && merged + qpt <= HESS_MERGE)
+					{
+						const int g2 = a.W.gate[gi + 1].g;
+						flush = (a.block[g2] != blk || wrow[g2] != wg);
+					}
 					for (unsigned q = threadIdx.x; q < (unsigned)Q; q += blockDim.x)
 					{
 						unsigned ex, ew, ey, ez;
@@ -1293,7 +1311,14 @@ __global__ void __launch_bounds__(256) k_hessian(Args<P> a, long nitems)
 							tile[ez] = P::madd2(G.c2, vy, G.c3, vz);
 						}
 					}
-					block_reduce8<P>(acc, s.red, hrow + (size_t)a.block[r.g] * 16, wrow[r.g], nred);
+					if (flush)
+					{
+						block_reduce8<P>(acc, s.red, hrow + (size_t)blk * 16, wg, nred);
+#pragma unroll
+						for (int e = 0; e < 8; e++) acc[e] = P::acc_zero();
+						merged = 0;
+					}
+					else __syncthreads();
 				}
 				if (pp < a.W.npass - 1) tile_store<P>(tile, kt, s, nlb, sh, false);
 				__syncthreads();
