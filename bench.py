@@ -58,6 +58,9 @@ def parse():
     ap.add_argument("--sample-columns", type=int, default=4096, help="column sample of --config grad18")
     ap.add_argument("--profile-columns", type=int, default=0,
                     help="small case for ncu: one evaluation over this many columns, no timing, then exit")
+    ap.add_argument("--profile-hessian", type=int, default=0,
+                    help="with --config hess14, for ncu: one mixed evaluation launched in chunks of this many "
+                         "columns (each chunk one k_hessian launch), no FP64 arm, no timing, then exit")
     return ap.parse_args()
 
 
@@ -371,6 +374,17 @@ def run_secondary(a):
     g, w, v, perms = workload(L, nl, a.trotter_steps)
     target = lib.target_circuit(g, w, L)
     ncols = 1 << L
+    if a.config == "hess14" and a.profile_hessian:
+        lib.set_precision(mgcu.PREC_MIXED)
+        lib.set_option(mgcu.OPT_CHUNK_COLUMNS, a.profile_hessian)
+        cg = np.array([v[l] for l in range(nl) for _ in range(L // 2)])
+        cw = np.array([[perms[l][2 * i], perms[l][2 * i + 1]] for l in range(nl) for i in range(L // 2)], np.int32)
+        rc, f, dg, H = lib.circuit_target_gradient_hessian(lib.mg_target_apply, target, cg, cw, L)
+        assert rc == 0, lib.last_error()
+        lib.set_option(mgcu.OPT_CHUNK_COLUMNS, 0)
+        lib.target_free(target)
+        print(json.dumps({"profile_hessian": a.profile_hessian, "L": L, "f": [f.real, f.imag]}))
+        return
     res = {}
     for name, prec in (("mixed", mgcu.PREC_MIXED), ("fp64", mgcu.PREC_FP64)):
         lib.set_precision(prec)
