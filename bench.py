@@ -58,6 +58,10 @@ def parse():
     ap.add_argument("--sample-columns", type=int, default=4096, help="column sample of --config grad18")
     ap.add_argument("--profile-columns", type=int, default=0,
                     help="small case for ncu: one evaluation over this many columns, no timing, then exit")
+    ap.add_argument("--hessian", default="per-gate", choices=["per-gate", "layer", "ti"],
+                    help="--config hess14: per-gate blocks (504 parameters), per-layer blocks "
+                         "(matchgate_brickwall_unitary_target_gradient_hessian, 72 parameters) or its "
+                         "translation-invariant variant")
     ap.add_argument("--profile-hessian", type=int, default=0,
                     help="with --config hess14, for ncu: one mixed evaluation launched in chunks of this many "
                          "columns (each chunk one k_hessian launch), no FP64 arm, no timing, then exit")
@@ -396,6 +400,16 @@ def run_secondary(a):
             dt = time.perf_counter() - t0
             assert rc == 0, lib.last_error()
             res[name] = {"evals_per_s": (c / ncols) / dt, "s_per_eval": dt * ncols / c, "f": f, "g": dv.reshape(-1)}
+        elif a.hessian != "per-gate":
+            # one block per layer (the reference's brickwall Hessian, 8 * nl real parameters),
+            # or its translation-invariant variant (one placement per layer, weighted)
+            ti = a.hessian == "ti"
+            lib.brickwall_target_gradient_hessian(lib.mg_target_apply, target, v[:1], perms[:1], L, ti=ti)   # warm-up
+            t0 = time.perf_counter()
+            rc, f, dv, H = lib.brickwall_target_gradient_hessian(lib.mg_target_apply, target, v, perms, L, ti=ti)
+            dt = time.perf_counter() - t0
+            assert rc == 0, lib.last_error()
+            res[name] = {"evals_per_s": 1 / dt, "s_per_eval": dt, "f": f, "g": dv.reshape(-1), "H": np.asarray(H)}
         else:
             # every gate of the brickwall its own parameter block: 8 * nl * L/2 real parameters
             cg = np.array([v[l] for l in range(nl) for _ in range(L // 2)])
@@ -412,13 +426,15 @@ def run_secondary(a):
     acc = {"rel_err_f_vs_fp64": abs(mx["f"] - fp["f"]) / abs(fp["f"]), "rel_err_grad_vs_fp64": rel(mx["g"], fp["g"])}
     if "H" in mx:
         acc["rel_err_hessian_vs_fp64"] = rel(mx["H"], fp["H"])
-    what = "gradient" if a.config == "grad18" else "gradient + per-gate Hessian"
+    what = "gradient" if a.config == "grad18" else {"per-gate": "gradient + per-gate Hessian",
+                                                     "layer": "gradient + per-layer Hessian",
+                                                     "ti": "gradient + translation-invariant per-layer Hessian"}[a.hessian]
     out = {"metric": f"{what} evals/s at L={L} (mixed vs FP64 GPU)", "value": mx["evals_per_s"], "unit": "evals/s",
            "n_gpus": 1, "higher_is_better": True, "dtype": "f32 float-float pairs, f64 final sums",
            "data": "synthetic (seeded Hubbard Trotter target, seeded near-identity fit)",
            "config": {"workload": f"L={L} spinful Hubbard Trotter target ({len(g)} gates), {nl}-layer brickwall fit "
                                   f"({nl * (L // 2)} gates), {what} over all 2^{L} columns",
-                      "real_parameters": 8 * nl * (L // 2) if a.config == "hess14" else 8 * nl,
+                      "real_parameters": 8 * nl * (L // 2) if a.config == "hess14" and a.hessian == "per-gate" else 8 * nl,
                       "L": L, "nlayers": nl, "target_gates": len(g)},
            "s_per_eval": {"mixed": mx["s_per_eval"], "fp64": fp["s_per_eval"]},
            "speedup_mixed_vs_fp64": fp["s_per_eval"] / mx["s_per_eval"], "accuracy": acc,
