@@ -273,6 +273,42 @@ def test_tiled_hessian_vs_oracle(lib, oracle):
     assert udist(h2, h2_o) < 1e-10
 
 
+@pytest.mark.parametrize("prec", [mgcu.PREC_FP64, mgcu.PREC_MIXED])
+def test_hessian_reduction_runs(lib, prec):
+    """Hessian items reduce once per run of gates with the same block and weight, capped at
+    64 quartets per thread: with 32 threads on a 2^11 tile (16 quartets per thread) a
+    six-gate layer is cut after four gates, with 256 threads (2 per thread) it is one run.
+    Both, and the translation-invariant weights, agree with each other; the uncapped path
+    is checked against the oracle by the golden and tiled Hessian tests."""
+    rng = np.random.default_rng(91)
+    L, nl = 12, 3
+    v = random_gates(nl, rng, unitary=True)
+    perms = brickwall_perms(L, nl, rng)
+    ulist = random_gates(4, rng, unitary=True)
+    uperms = brickwall_perms(L, 4, rng)
+    t = lib.target_brickwall(ulist, uperms, L)
+    out = {}
+    lib.set_precision(prec)
+    try:
+        for threads in (0, 32, 64):
+            lib.set_option(mgcu.OPT_THREADS, threads)
+            for ti in (False, True):
+                rc, f, dv, h = lib.brickwall_target_gradient_hessian(lib.mg_target_apply, t, v, perms, L, ti=ti)
+                assert rc == 0, lib.last_error()
+                out[threads, ti] = (f, dv, h)
+    finally:
+        lib.set_option(mgcu.OPT_THREADS, 0)
+        lib.set_precision(mgcu.PREC_FP64)
+        lib.target_free(t)
+    tol = 1e-12 if prec == mgcu.PREC_FP64 else 1e-9
+    for ti in (False, True):
+        f0, dv0, h0 = out[0, ti]
+        for threads in (32, 64):
+            f, dv, h = out[threads, ti]
+            assert abs(f - f0) < tol * abs(f0) and udist(dv, dv0) < tol * np.max(np.abs(dv0))
+            assert udist(h, h0) < tol * np.max(np.abs(h0))
+
+
 def test_per_gate_circuit_gradient_and_hessian(lib, oracle, helpers):
     rng = np.random.default_rng(12)
     L, ng = 6, 8
