@@ -113,6 +113,21 @@ def workload(L, nlayers, nsteps, seed=3):
 TARGET_DRAM_BYTES_PER_COLUMN = {16: (11.680262e9 + 12.663491e9) / 608}
 
 
+def hbm_view(traffic, launch_s):
+    """the dominant kernel against the measured HBM copy bandwidth (MEASURED_PEAKS.json,
+    else the 6800 GB/s fallback): DRAM bytes per launch over the launch time"""
+    if not traffic:
+        return None
+    peak, src = 6800.0, "fallback"
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as fh:
+            peak, src = float(json.load(fh)["hbm_gbs"]), "measured"
+    except (OSError, ValueError, KeyError):
+        pass
+    gbs = traffic / launch_s / 1e9
+    return {"achieved_gbs": gbs, "peak_gbs": peak, "frac": gbs / peak, "peak_source": src}
+
+
 def alg_flops(L, gu, gw, ncols):
     """algorithmic real flops of target+gradient over ncols columns, counted on the parity
     sector S = 2^(L-1): 14 per amplitude and forward gate, 44 per amplitude and fitted gate
@@ -349,7 +364,8 @@ def run_gb300(a):
                      "peak_source": "FP32 FMA microkernel of this library, measured in this run "
                                     "(MEASURED_PEAKS.json holds HBM and bf16 tensor peaks only)",
                      "traffic_source": "ncu dram__bytes_read+write per column, profiles/k_target_mixed_hubbard_L16.md, x columns per launch",
-                     "fp64_peak_tflops": fp64_peak / 1e3},
+                     "fp64_peak_tflops": fp64_peak / 1e3,
+                     "hbm": hbm_view(traffic, tk_avg_s)},
         "fp64_gpu": {"value": fp64_value, "unit": UNIT, "sample_columns": c, "extrapolated_from_sample": True,
                      "speedup_of_timed_precision": value / world / fp64_value},
         "accuracy": {"rel_err_f_vs_fp64": rel_f, "rel_err_grad_vs_fp64": rel_g, "columns": c,
