@@ -322,6 +322,15 @@ __device__ __forceinline__ void quartet(const GateRec& r, unsigned q, int tpar, 
 	}
 }
 
+// L2 prefetch of [p, p + bytes) by the whole block, one 128-byte line per request
+// (generic addresses inside one allocation)
+__device__ __forceinline__ void l2_prefetch_block(const void* p, size_t bytes)
+{
+	const char* c = static_cast<const char*>(p);
+	for (size_t o = (size_t)threadIdx.x * 128; o < bytes; o += (size_t)blockDim.x * 128)
+		asm volatile("prefetch.L2 [%0];" :: "l"(c + o));
+}
+
 template <class P> struct Red;
 template <> struct Red<PrecD>
 {
@@ -1064,11 +1073,17 @@ __device__ __forceinline__ void w_column(const Args<P>& a, long b, const typenam
 			{
 				const unsigned nlb = nl_base(pr, tau);
 				const int tpar = (__popcll(nlb) + par) & 1;
+				// the cached inputs of this tile's gates (tile order, 2^kt contiguous
+				// amplitudes each) go to L2 one gate ahead of their reads
+				if (tl && pr.gend > pr.gbeg)
+					l2_prefetch_block(cache + (size_t)a.W.gate[pr.gend - 1].g * S + ((size_t)tau << kt), sizeof(T) << kt);
 				tile_load<P>(tile, kt, s, nlb, (p == a.W.npass - 1) ? dsrc : su);
 				__syncthreads();
 				for (int gi = pr.gend - 1; gi >= pr.gbeg; gi--)
 				{
 					const GateRec r = a.W.gate[gi];
+					if (tl && gi > pr.gbeg)
+						l2_prefetch_block(cache + (size_t)a.W.gate[gi - 1].g * S + ((size_t)tau << kt), sizeof(T) << kt);
 					const Gate8<T> G = load_gate(a.wm, r.g);
 					const T* cg = cache + (size_t)r.g * S;
 					T* dg = dcache ? dcache + (size_t)r.g * S : nullptr;
