@@ -1,7 +1,7 @@
 """ctypes wrapper of the oracle (test infrastructure only).
 
 Loads ``oracle/_build/libmgoracle.so`` (the C restatement, built by
-``oracle/build.py``) and exposes numpy-facing helpers.  Gates are numpy complex128
+``oracle/build_oracle.py``) and exposes numpy-facing helpers.  Gates are numpy complex128
 arrays of shape (n, 8): entries 0..3 the row-major center block, 4..7 the corner
 block -- the memory layout of the reference's ``struct matchgate``.  Permutations
 are int32 arrays of shape (nlayers, L).
