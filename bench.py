@@ -192,6 +192,18 @@ def cpu_baseline(g, w, v, perms, L, budget_s, nthreads=0):
     return (ncols / float(1 << L)) / dt, nthreads, ncols, dt
 
 
+def cpu_baseline_line(g, w, v, perms, L, budget_s, ncols):
+    """the bench line's cpu_baseline: the port on all host cores (OpenMP over basis columns,
+    as the reference's parallel drivers split the trace), and beside it on one core (the
+    reference's gradient path is serial as shipped, src/matchgate_target.c:212-302)"""
+    cv, cores, cc, cs = cpu_baseline(g, w, v, perms, L, budget_s)
+    c1, _, n1, s1 = cpu_baseline(g, w, v, perms, L, budget_s / 4, nthreads=1)
+    return {"value": cv, "unit": UNIT, "cores": cores, "kind": "port",
+            "sample": f"{cc} of {ncols} basis columns in {cs:.1f} s, scaled to one full evaluation",
+            "single_core": {"value": c1, "unit": UNIT, "cores": 1,
+                            "sample": f"{n1} of {ncols} basis columns in {s1:.1f} s, scaled to one full evaluation"}}
+
+
 def run_reference(a):
     rank, world, _ = dist_env()
     if rank != 0:
@@ -374,9 +386,7 @@ def run_gb300(a):
         "resident_target": resident,
     }
     if rank == 0 and world == 1 and not a.no_cpu:
-        cv, cores, cc, cs = cpu_baseline(g, w, v, perms, L, a.cpu_seconds)
-        out["cpu_baseline"] = {"value": cv, "unit": UNIT, "cores": cores, "kind": "port",
-                               "sample": f"{cc} of {ncols} basis columns in {cs:.1f} s, scaled to one full evaluation"}
+        out["cpu_baseline"] = cpu_baseline_line(g, w, v, perms, L, a.cpu_seconds, ncols)
     lib.lib.mg_plan_free(mgcu.P(plan))
     lib.target_free(target)
     if rank == 0:
