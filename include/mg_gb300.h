@@ -215,17 +215,20 @@ double mg_measure_fp64_peak_gflops(void);
  * For callers that cannot allocate GPU memory while they run -- a host that hands all
  * device memory to its own pool allocator up front, a real-time loop where the implicit
  * synchronisation of cudaMalloc/cudaFree is not acceptable, or a process whose memory
- * budget is fixed at start-up.  Computes f and the per-layer gate gradients of a brickwall
- * (vlist, perms) against a target given as a gate list (ugates on uwires[2g], uwires[2g+1]),
- * like matchgate_brickwall_unitary_target_and_gradient with a GPU target, in complex128.
+ * budget is fixed at start-up.  Computes, in complex128, f = -tr(U^dagger W) and the raw
+ * (holomorphic, unprojected) gradient of f with respect to each layer's shared gate, summed
+ * over the layer's gates, for a brickwall W (vlist, perms: every perms[i] a permutation of
+ * the qubits) against a target U given as a gate list (ugates on uwires[2g], uwires[2g+1]).
  * It calls no cudaMalloc, cudaFree or other allocating routine, on the device or the host:
  * all workspace lives in one fixed array that every GPU loading this library reserves
- * until the process exits (about 35 MB).  Limits: even 4 <= nqubits <= 10,
- * nlayers * nqubits / 2 <= 64 fitted gates, ungates <= 4096; larger sizes are rejected
- * with MG_ERR_ARG (-6) and a message.  The first call on a device looks up the array's
- * device address; make that first call before any stream capture.  All calls share the
- * array (the library clears what must start at zero), so calls that overlap on the GPU,
- * for example from several processes on one device, race. */
+ * until the process exits (about 35 MB; one copy per process and GPU).  Limits: even
+ * 4 <= nqubits <= 10, nlayers * nqubits / 2 <= 64 fitted gates, ungates <= 4096; larger
+ * sizes and invalid wirings are rejected with MG_ERR_ARG (-6) and a message.  The first
+ * call on a device looks up the array's device address; make that first call before any
+ * stream capture.  All calls of a process share the array, which keeps the last call's
+ * contents (the library clears what must start at zero).  The library's lock serialises
+ * the calls and each call waits for its GPU work before it returns, so two calls never
+ * overlap on the GPU; GPU work of two calls that did overlap would race on the array. */
 int mg_noalloc_brickwall_target_and_gradient(const struct matchgate ugates[], int ungates, const int uwires[],
 	const struct matchgate vlist[], int nlayers, int nqubits, const int* perms[], numeric* fval, struct matchgate dvlist[]);
 

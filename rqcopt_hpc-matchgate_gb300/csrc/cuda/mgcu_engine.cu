@@ -2838,13 +2838,23 @@ extern "C" int mg_noalloc_brickwall_target_and_gradient(const void* ugates, int 
 			mg_set_error("mg_noalloc_brickwall_target_and_gradient: invalid wires of target gate %d", g / 2);
 			return MG_ERR_ARG;
 		}
+	// each layer's wiring must be a permutation: a gate whose two wires coincide has no
+	// quartet layout (the regular plans reject it the same way)
 	for (int i = 0; i < nlayers; i++)
+	{
+		unsigned seen = 0;
 		for (int p = 0; p < L; p++)
-			if (perms[i][p] < 0 || perms[i][p] >= L)
+		{
+			const int q = perms[i][p];
+			if (q < 0 || q >= L || (seen >> q) & 1u)
 			{
-				mg_set_error("mg_noalloc_brickwall_target_and_gradient: invalid permutation of layer %d", i);
+				mg_set_error("mg_noalloc_brickwall_target_and_gradient: invalid permutation of layer %d "
+					"(wire %d out of range or repeated)", i, q);
 				return MG_ERR_ARG;
 			}
+			seen |= 1u << q;
+		}
+	}
 	mgcu_lock();
 	MgcuContext* c = mgcu_ctx();
 	if (!c) { mgcu_unlock(); return MG_ERR_DEVICE; }

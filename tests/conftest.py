@@ -22,7 +22,9 @@ for p in (os.path.join(ROOT, "oracle"), PKG, os.path.dirname(os.path.abspath(__f
     if p not in sys.path:
         sys.path.insert(0, p)
 
-REF_SRC = os.environ.get("MG_REFERENCE_SRC", "/root/reference/src")
+# where the reference sources lie: the oracle recipe owns that default (MG_REFERENCE_SRC overrides);
+# tests that need them skip when they are absent (as on a machine without the reference)
+from build_oracle import REF_SRC  # noqa: E402
 
 
 def pytest_configure(config):

@@ -22,7 +22,9 @@ import types
 import numpy as np
 
 HERE = os.path.dirname(os.path.abspath(__file__))
-REF = sys.argv[1] if len(sys.argv) > 1 else "/root/reference"
+REF = sys.argv[1] if len(sys.argv) > 1 else os.environ.get("MG_REFERENCE", "")
+if not REF:
+    sys.exit("usage: gen_golden.py <reference checkout> (or set MG_REFERENCE)")
 REF_TEST = os.path.join(REF, "test")
 
 CAPTURED = {}

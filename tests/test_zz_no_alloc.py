@@ -28,7 +28,9 @@ def _noalloc(lib, ugates, uwires, vlist, perms, L):
     return rc, f[0], dv
 
 
-@pytest.mark.parametrize("L,nl,ng", [(8, 4, 60), (10, 5, 200)])
+# L=4 and L=6 run one warp per block (2 and 8 quartets per gate): the strided backward
+# loop and the single-warp block reduction
+@pytest.mark.parametrize("L,nl,ng", [(4, 2, 10), (6, 3, 30), (8, 4, 60), (10, 5, 200)])
 def test_noalloc_matches_regular_entry_point(mglib, L, nl, ng):
     lib = mglib
     lib.set_precision(mgcu.PREC_FP64)
@@ -58,3 +60,14 @@ def test_noalloc_rejects_sizes_beyond_its_array(mglib):
                          T.brickwall_perms(L, 2), L)
     assert rc == -6
     assert "fixed workspace" in mglib.last_error()
+
+
+def test_noalloc_rejects_repeated_wires(mglib):
+    """a layer whose wiring repeats a qubit is rejected before anything reaches the GPU"""
+    rng = np.random.default_rng(4)
+    L = 8
+    perms = T.brickwall_perms(L, 2).copy()
+    perms[1, 7] = perms[1, 6]
+    rc, f, dv = _noalloc(mglib, random_gates(4, rng), np.array([[0, 1]] * 4, np.int32), random_gates(2, rng), perms, L)
+    assert rc == -6
+    assert "invalid permutation of layer 1" in mglib.last_error()
