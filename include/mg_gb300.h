@@ -32,9 +32,15 @@ int mg_get_precision(void);
  * CTAS_PER_SM: resident blocks per SM for the persistent grid; TARGET_TILE_BITS and
  * TARGET_THREADS: the same two for the sweep of a GPU circuit target (default: TILE_BITS
  * and its block size; at most 2^13 amplitudes of 16 B and 512 threads); TARGET_COLUMNS: 2 sweeps
- * two basis columns of equal parity per block (256 threads), sharing the per-gate work. */
+ * two basis columns of equal parity per block (256 threads), sharing the per-gate work.
+ * TRANSLATIONAL_INVARIANCE: 1 makes matchgate_brickwall_unitary_target_gradient_hessian, its
+ * parallel_ twin, matchgate_brickwall_unitary_target_gradient_vector_hessian_matrix and
+ * mg_optimize_brickwall use the translation-invariant Hessian -- what building the reference
+ * with -DTRANSLATIONAL_INVARIANCE does to the same entry points (src/matchgate_target.c:478,
+ * 715, 819); 0 (default) is the reference's plain build. */
 enum { MG_OPT_TILE_BITS = 1, MG_OPT_THREADS = 2, MG_OPT_CHUNK_COLUMNS = 3, MG_OPT_CTAS_PER_SM = 4,
-       MG_OPT_TARGET_TILE_BITS = 5, MG_OPT_TARGET_THREADS = 6, MG_OPT_TARGET_COLUMNS = 7 };
+       MG_OPT_TARGET_TILE_BITS = 5, MG_OPT_TARGET_THREADS = 6, MG_OPT_TARGET_COLUMNS = 7,
+       MG_OPT_TRANSLATIONAL_INVARIANCE = 8 };
 int mg_set_option(int option, long value);
 long mg_get_option(int option);
 

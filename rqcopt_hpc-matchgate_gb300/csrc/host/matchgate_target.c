@@ -396,6 +396,10 @@ static int* identity_blocks(int n)
 	return b;
 }
 
+/* the translation-invariant Hessian in place of the plain one: the reference's build flag
+ * TRANSLATIONAL_INVARIANCE (src/matchgate_target.c:478,715,819) as a runtime option */
+static int ti_build(void) { return mgcu_option(MG_OPT_TRANSLATIONAL_INVARIANCE_ID) != 0; }
+
 static int brickwall_eval(linear_func ufunc, void* udata, const struct matchgate vlist[], int nlayers, int L, const int* perms[],
 	int want_grad, int want_hess, int ti, long b0, long b1, numeric* fval, struct matchgate* dvlist, numeric* hess, double* grad_vec, double* H)
 {
@@ -486,7 +490,7 @@ int matchgate_brickwall_unitary_target_gradient_hessian(linear_func ufunc, void*
 	const struct matchgate vlist[], const int nlayers, const int nqubits, const int* perms[],
 	numeric* fval, struct matchgate dvlist[], numeric* hess)
 {
-	return brickwall_eval(ufunc, udata, vlist, nlayers, nqubits, perms, 1, 1, 0, 0, -1, fval, dvlist, hess, NULL, NULL);
+	return brickwall_eval(ufunc, udata, vlist, nlayers, nqubits, perms, 1, 1, ti_build(), 0, -1, fval, dvlist, hess, NULL, NULL);
 }
 
 int matchgate_ti_brickwall_unitary_target_gradient_hessian(linear_func ufunc, void* udata,
@@ -507,7 +511,7 @@ int matchgate_brickwall_unitary_target_gradient_vector_hessian_matrix(linear_fun
 	const struct matchgate vlist[], const int nlayers, const int nqubits, const int* perms[],
 	numeric* fval, double* grad_vec, double* H)
 {
-	return brickwall_eval(ufunc, udata, vlist, nlayers, nqubits, perms, 1, 1, 0, 0, -1, fval, NULL, NULL, grad_vec, H);
+	return brickwall_eval(ufunc, udata, vlist, nlayers, nqubits, perms, 1, 1, ti_build(), 0, -1, fval, NULL, NULL, grad_vec, H);
 }
 
 int matchgate_brickwall_unitary_target_and_projected_gradient(linear_func ufunc, void* udata,

@@ -34,7 +34,8 @@ static int plans_make(plans_t* p, void* target, const struct matchgate* v, int n
 	plans_free(p);
 	const int old = mg_get_precision();
 	mg_set_precision(prec);
-	p->h = mg_plan_brickwall(mg_target_apply, target, v, nl, L, perms, MG_EVAL_HESSIAN);
+	const int ti = mgcu_option(MG_OPT_TRANSLATIONAL_INVARIANCE_ID) != 0;
+	p->h = mg_plan_brickwall(mg_target_apply, target, v, nl, L, perms, MG_EVAL_HESSIAN | (ti ? MG_EVAL_TI : 0));
 	p->f = p->h ? mg_plan_brickwall(mg_target_apply, target, v, nl, L, perms, MG_EVAL_TARGET) : NULL;
 	mg_set_precision(old);
 	p->prec = prec;

@@ -30,7 +30,7 @@ void mgcu_lock(void) { pthread_mutex_lock(&g_lock); }
 void mgcu_unlock(void) { pthread_mutex_unlock(&g_lock); }
 
 static int g_precision = MG_PREC_FP64;
-static long g_options[8];
+static long g_options[MG_NOPTIONS + 1];
 
 int mg_set_precision(int precision)
 {

@@ -33,7 +33,8 @@ extern "C" {
 #define MG_OPT_TARGET_TILE_BITS_ID 5
 #define MG_OPT_TARGET_THREADS_ID   6
 #define MG_OPT_TARGET_COLUMNS_ID   7
-#define MG_NOPTIONS             7
+#define MG_OPT_TRANSLATIONAL_INVARIANCE_ID 8
+#define MG_NOPTIONS             8
 
 /* ---- runtime ---- */
 void mg_set_error(const char* fmt, ...);

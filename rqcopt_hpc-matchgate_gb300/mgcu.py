@@ -23,6 +23,7 @@ DEFAULT_LIB = os.path.join(HERE, "_build", "libmgcu.so")
 PREC_FP64, PREC_MIXED, PREC_FP32 = 0, 1, 2
 OPT_TILE_BITS, OPT_THREADS, OPT_CHUNK_COLUMNS, OPT_CTAS_PER_SM = 1, 2, 3, 4
 OPT_TARGET_TILE_BITS, OPT_TARGET_THREADS, OPT_TARGET_COLUMNS = 5, 6, 7
+OPT_TRANSLATIONAL_INVARIANCE = 8
 EVAL_TARGET, EVAL_GRADIENT, EVAL_HESSIAN, EVAL_TI = 0, 1, 2, 4
 
 P = C.c_void_p
@@ -522,6 +523,13 @@ class MatchgateLib:
         v = gates_arr(v); z = gates_arr(z); r = np.zeros(8)
         self.lib.tangent_matchgate_to_real(_p(v), _p(z), _p(r))
         return r
+
+    def project_gradient(self, vlist, dvlist):
+        """Riemannian gradient vector [8 nlayers] of raw layer gradients: each conjugated and
+        mapped by tangent_matchgate_to_real (reference src/matchgate_target.c:902-908)"""
+        v = gates_arr(vlist)
+        dv = gates_arr(dvlist)
+        return np.concatenate([self.tangent_to_real(v[i], np.conj(dv[i])) for i in range(len(v))])
 
     def retract(self, u, eta):
         u = gates_arr(u); eta = np.ascontiguousarray(eta, np.float64); out = np.zeros((1, 8), cd)

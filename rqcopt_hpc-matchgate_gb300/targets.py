@@ -134,3 +134,50 @@ def circuit_unitary(gates, wires, L):
         T = (G4 @ T).reshape([2, 2] + [2] * (L - 2) + [n])
         M = np.moveaxis(T, [0, 1], [i, j]).reshape(n, n)
     return M
+
+
+def merge_runs(indices, coeffs):
+    """neighbouring layers of the same term merged (their coefficients added)"""
+    mi, mc = [], []
+    for i, c in zip(indices, coeffs):
+        if mi and mi[-1] == i:
+            mc[-1] += c
+        else:
+            mi.append(i); mc.append(c)
+    return mi, mc
+
+
+def suzuki_rule(nterms, k):
+    """Suzuki's symmetric product rule of order 2k over nterms terms, as (term index,
+    coefficient) per layer with neighbouring layers of one term merged: S_2 = the terms
+    forward then backward with coefficient 1/2 each, S_2k = S_2k-2 at p, p, 1-4p, p, p with
+    p = 1/(4 - 4^(1/(2k-1))) (M. Suzuki, Phys. Lett. A 146, 319 (1990); the reference's
+    generator, test/rqcopt_matfree/splitting_method.py:161-193)"""
+    if k == 1:
+        return merge_runs(list(range(nterms)) + list(range(nterms))[::-1], [0.5] * (2 * nterms))
+    p = 1.0 / (4.0 - 4.0 ** (1.0 / (2 * k - 1)))
+    i1, c1 = suzuki_rule(nterms, k - 1)
+    return merge_runs(i1 * 5, [w * c for w in (p, p, 1 - 4 * p, p, p) for c in c1])
+
+
+def spinless_hubbard_gate(J, g, tau):
+    """exp(-i tau h) for the two-site term h = -J (|01><10| + |10><01|) + g |11><11| of the
+    spinless Fermi-Hubbard chain (Jordan-Wigner, nearest neighbours): center block
+    exp(i tau J X), corner block diag(1, exp(-i tau g))"""
+    c, s = np.cos(J * tau), np.sin(J * tau)
+    return _gate([[c, 1j * s], [1j * s, c]], np.diag([1.0, np.exp(-1j * g * tau)]))
+
+
+def spinless_hubbard_brickwall(L, J, g, t, nsteps, order):
+    """The reference's benchmark circuits (benchmark_hpc/spl_hubbard1d_bench_init.py:24-118):
+    nsteps steps of the order-`order` Suzuki rule over time t for the spinless 1-D Hubbard
+    model on L sites, terms = even bonds (pairs (0,1),(2,3),...) and odd bonds ((1,2),...,
+    (L-1,0), periodic wiring), neighbouring layers of one term merged across steps.  Returns
+    (gates [nlayers, 8], perms [nlayers, L]): one matchgate per layer on all L/2 pairs."""
+    i1, c1 = suzuki_rule(2, order // 2)
+    idx, cf = merge_runs(i1 * nsteps, c1 * nsteps)
+    dt = t / nsteps
+    gates = np.array([spinless_hubbard_gate(J, g, c * dt) for c in cf])
+    even, odd = np.arange(L), np.roll(np.arange(L), -1)
+    perms = np.array([even if i == 0 else odd for i in idx], dtype=np.int32)
+    return gates, perms

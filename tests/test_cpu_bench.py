@@ -38,3 +38,23 @@ def test_command_line(monkeypatch, argv, want):
     a = bench.parse()
     assert (a.config, a.hessian, a.steps, a.warmup) == want
     assert a.gpus == 1 and a.impl == "gb300"
+
+
+def test_reference_arm_line(monkeypatch, capsys):
+    """--impl reference on a small instance: ms_per_step is the wall time each step really
+    took (steps x ms_per_step fits inside the run), the column sample is stated, and the
+    config dict is the one the GPU arm prints"""
+    import json
+    import time
+    monkeypatch.setattr(sys, "argv", ["bench.py", "--impl", "reference", "--L", "8", "--layers", "4",
+                                      "--trotter-steps", "2", "--steps", "2", "--warmup", "3"])
+    t0 = time.perf_counter()
+    bench.main()
+    wall = time.perf_counter() - t0
+    line = json.loads(capsys.readouterr().out.strip().splitlines()[-1])
+    assert line["impl"] == "reference" and line["steps"] == 2 and line["warmup"] == 3
+    assert line["steps"] * line["ms_per_step"] / 1e3 <= wall
+    assert 0 < line["columns_per_step"] <= 256
+    g, w, v, perms = bench.workload(8, 4, 2)
+    assert line["config"] == bench.headline_config(8, 4, len(g), 2)
+    assert abs(line["value"] - line["columns_per_step"] / 256 / (line["ms_per_step"] / 1e3)) < 1e-9 * line["value"]

@@ -60,3 +60,29 @@ def test_suzuki_orders_approach_exact_evolution(mglib, nsites):
 def test_bad_arguments(mglib):
     assert mglib.lib.mg_hubbard_trotter_circuit(1, 1.0, 4.0, 0.25, 4, 2, None, None, 0) < 0
     assert mglib.lib.mg_hubbard_trotter_circuit(4, 1.0, 4.0, 0.25, 4, 3, None, None, 0) < 0
+
+
+def test_spinless_hubbard_brickwall_matches_generator_conventions():
+    """the published benchmark's circuits: 5 layers (order 2, 2 steps) and 601 layers (order 6,
+    12 steps); each layer gate is expm(-i tau h) of the two-site term with its blocks taken in
+    struct matchgate order (center on |01>,|10>, corner on |00>,|11>)"""
+    import numpy as np
+    from scipy.linalg import expm
+    import targets as T
+    v, p = T.spinless_hubbard_brickwall(16, 1.0, 1.5, 1.0, 2, 2)
+    u, up = T.spinless_hubbard_brickwall(16, 1.0, 1.5, 1.0, 12, 6)
+    assert len(v) == 5 and len(u) == 601 and up.shape == (601, 16)
+    assert [int(x[0]) for x in p] == [0, 1, 0, 1, 0] and list(p[1]) == list(range(1, 16)) + [0]
+    _, cf = T.suzuki_rule(2, 1)
+    assert np.allclose(cf, [0.5, 1.0, 0.5])
+    n = np.array([[0, 0], [0, 1]]); a = np.array([[0, 1], [0, 0]])
+    h = -1.0 * (np.kron(a.T, a) + np.kron(a, a.T)) + 1.5 * np.kron(n, n)
+    for tau in (0.25, -0.3, 0.5):
+        X = expm(-1j * tau * h)
+        gate = T.spinless_hubbard_gate(1.0, 1.5, tau)
+        assert np.allclose(gate[:4].reshape(2, 2), X[1:3, 1:3], atol=1e-15)
+        assert np.allclose(gate[4:].reshape(2, 2), X[np.ix_([0, 3], [0, 3])], atol=1e-15)
+    # coefficients of one order-6 step sum to 1 per term
+    i6, c6 = T.suzuki_rule(2, 3)
+    assert len(i6) == 51
+    assert abs(sum(c for i, c in zip(i6, c6) if i == 0) - 1) < 1e-13 and abs(sum(c for i, c in zip(i6, c6) if i == 1) - 1) < 1e-13
