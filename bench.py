@@ -17,6 +17,7 @@ OpenMP over basis columns) on the host's cores on a bounded column sample.
 """
 import argparse
 import json
+import math
 import os
 import statistics
 import subprocess
@@ -121,11 +122,11 @@ def headline_config(L, nl, gu, trotter_steps):
 
 
 # DRAM bytes (read + write) of the target-sweep kernel per basis column: ncu
-# dram__bytes_read.sum + dram__bytes_write.sum of one k_target<PrecX> launch over 608 columns
-# of this workload (L=16, float-float).  The kernel's traffic is its output columns plus the
-# tile round trips that miss L2, both proportional to the columns, so per-launch traffic =
-# this x columns per launch.
-TARGET_DRAM_BYTES_PER_COLUMN = {16: (11.680262e9 + 12.663491e9) / 608}
+# dram__bytes_read.sum + dram__bytes_write.sum of one k_target_w<PrecX> launch over 912 columns
+# of this workload (L=16, float-float, two columns per resident block).  The kernel's traffic
+# is its output columns plus the tile round trips that miss L2, both proportional to the
+# columns, so per-launch traffic = this x columns per launch.
+TARGET_DRAM_BYTES_PER_COLUMN = {16: (23.944726e9 + 20.012690e9) / 912}
 
 
 def hbm_view(traffic, launch_s):
@@ -391,9 +392,14 @@ def run_gb300(a):
     # dominant kernel: the target sweep (k_target), timed by CUDA events around each launch
     cols_per_launch = ncols * a.steps / tk_n
     gu_run = lib.lib.mg_target_sweep_gates(mgcu.P(target))   # gates the sweep applies (fermionic swaps relabelled away)
-    tk_flops = float(cols_per_launch) * (1 << (L - 1)) * 14 * gu_run
+    # amplitude-columns the sweep visits per launch: the whole parity sector of every column,
+    # or (Hamming-weight-conserving target) the amplitudes of the column's weight only:
+    # sum_b C(L, |b|) = C(2L, L) over all 2^L columns
+    weight = bool(lib.lib.mg_target_conserves_weight(mgcu.P(target)))
+    sector_units = float(cols_per_launch) * (1 << (L - 1))
+    live_units = float(math.comb(2 * L, L)) * cols_per_launch / ncols if weight else sector_units
     tk_avg_s = tk_ms / 1e3 / tk_n
-    achieved = tk_flops / tk_avg_s / 1e12
+    achieved = live_units * 14 * gu_run / tk_avg_s / 1e12
     bpc = TARGET_DRAM_BYTES_PER_COLUMN.get(L) if a.precision == "mixed" else None
     traffic = bpc * cols_per_launch if bpc else None
     out = {
@@ -413,14 +419,20 @@ def run_gb300(a):
                      "kernel": "k_target (target sweep)", "kernel_launches": tk_n,
                      "kernel_ms_per_launch": tk_avg_s * 1e3, "kernel_share_of_step": tk_ms / total_ms,
                      "columns_per_launch": cols_per_launch,
-                     "achieved_is": "algorithmic complex-arithmetic flops of the target sweep (14 per parity-sector "
+                     "achieved_is": "algorithmic complex-arithmetic flops of the target sweep (14 per visited "
+                                    "amplitude and applied gate) per second of k_target; the target conserves the "
+                                    "Hamming weight, so the sweep visits C(2L, L) amplitude-columns per trace, the "
+                                    "nonzero ones, not the 2^(2L-1) of the parity sectors" if weight else
+                                    "algorithmic complex-arithmetic flops of the target sweep (14 per parity-sector "
                                     "amplitude and applied gate) per second of k_target",
+                     "visited_amplitudes_per_launch": live_units,
+                     "parity_sector_equivalent_tflops": sector_units * 14 * gu_run / tk_avg_s / 1e12,
                      "target_gates_applied": gu_run,
                      "step_achieved": achieved_step,
                      "peak_source": "FP32 FMA microkernel of this library, measured in this run "
                                     "(MEASURED_PEAKS.json holds HBM and bf16 tensor peaks only)",
-                     "traffic_source": "ncu dram__bytes_read.sum + dram__bytes_write.sum of one k_target launch over "
-                                       "608 columns of this workload, per column, x columns per launch",
+                     "traffic_source": "ncu dram__bytes_read.sum + dram__bytes_write.sum of one k_target_w launch over "
+                                       "912 columns of this workload, per column, x columns per launch",
                      "fp64_peak_tflops": fp64_peak / 1e3,
                      "hbm": hbm_view(traffic, tk_avg_s)},
         "fp64_gpu": fp64,

@@ -37,10 +37,13 @@ int mg_get_precision(void);
  * parallel_ twin, matchgate_brickwall_unitary_target_gradient_vector_hessian_matrix and
  * mg_optimize_brickwall use the translation-invariant Hessian -- what building the reference
  * with -DTRANSLATIONAL_INVARIANCE does to the same entry points (src/matchgate_target.c:478,
- * 715, 819); 0 (default) is the reference's plain build. */
+ * 715, 819); 0 (default) is the reference's plain build.
+ * TARGET_DENSE: 1 sweeps every amplitude of a GPU circuit target even when all its gates
+ * conserve the Hamming weight (by default such targets are swept on the amplitudes of the
+ * basis column's weight only; both give bit-identical results). */
 enum { MG_OPT_TILE_BITS = 1, MG_OPT_THREADS = 2, MG_OPT_CHUNK_COLUMNS = 3, MG_OPT_CTAS_PER_SM = 4,
        MG_OPT_TARGET_TILE_BITS = 5, MG_OPT_TARGET_THREADS = 6, MG_OPT_TARGET_COLUMNS = 7,
-       MG_OPT_TRANSLATIONAL_INVARIANCE = 8 };
+       MG_OPT_TRANSLATIONAL_INVARIANCE = 8, MG_OPT_TARGET_DENSE = 9 };
 int mg_set_option(int option, long value);
 long mg_get_option(int option);
 
@@ -68,6 +71,13 @@ int mg_target_set_resident(void* udata, int enable);
  * restore the qubit order; the other gates then carry Jordan-Wigner strings), plus
  * any controlled-Z left over.  -1 for a dense target or an invalid handle. */
 int mg_target_sweep_gates(void* udata);
+/* 1 when every gate of a circuit target conserves the Hamming weight (no corner block mixes
+ * |00> and |11>: hopping and interaction terms of particle-conserving Hamiltonians, fermionic
+ * swaps).  U e_b then has nonzero amplitudes only at indices of the weight of b, and the GPU
+ * sweep visits only those (unless MG_OPT_TARGET_DENSE is set): C(2L, L) amplitude-columns per
+ * trace instead of 2^(2L-1), with bit-identical results.  0 otherwise (also for dense
+ * targets), -1 for an invalid handle. */
+int mg_target_conserves_weight(void* udata);
 
 /* ---------------------------------------------------------------------------------
  * Native trust-region fit (the loop of riemannian_trust_region_optimize_hmat,

@@ -136,6 +136,16 @@ struct PrecD
 		const double xr = ra ? x.y : x.x, xi = ra ? x.x : x.y, yr = rb ? y.y : y.x, yi = rb ? y.x : y.y;
 		return make_double2(fma(a.x, xr, b.x * yr), fma(a.y, xi, b.y * yi));
 	}
+	// symmetric hop block [[c, i s], [i s, c]] (c, s real) on the pair (a, b), its
+	// off-diagonal entries negated when sg == 1; c0 and c1 are the staged block entries
+	// (real c stored as (c, c), imaginary i s as (-s, s))
+	__device__ static void hop(T c0, T c1, unsigned sg, T& a, T& b)
+	{
+		const double c = c0.x, s = __longlong_as_double(__double_as_longlong(c1.y) ^ ((long long)sg << 63));
+		const T x = a, y = b;
+		a = make_double2(fma(c, x.x, -s * y.y), fma(c, x.y, s * y.x));
+		b = make_double2(fma(c, y.x, -s * x.y), fma(c, y.y, s * x.x));
+	}
 	__device__ static Acc acc_zero() { Acc a; a.re = 0; a.im = 0; return a; }
 	__device__ static void acc_mul_add(Acc& s, T d, T x)
 	{
@@ -182,6 +192,13 @@ struct PrecF
 	{
 		const float xr = ra ? x.y : x.x, xi = ra ? x.x : x.y, yr = rb ? y.y : y.x, yi = rb ? y.x : y.y;
 		return make_float2(fmaf(a.x, xr, b.x * yr), fmaf(a.y, xi, b.y * yi));
+	}
+	__device__ static void hop(T c0, T c1, unsigned sg, T& a, T& b)
+	{
+		const float c = c0.x, s = __uint_as_float(__float_as_uint(c1.y) ^ (sg << 31));
+		const T x = a, y = b;
+		a = make_float2(fmaf(c, x.x, -s * y.y), fmaf(c, x.y, s * y.x));
+		b = make_float2(fmaf(c, y.x, -s * x.y), fmaf(c, y.y, s * x.x));
 	}
 	__device__ static Acc acc_zero() { Acc a; a.rh = a.rl = a.ih = a.il = 0.f; return a; }
 	__device__ static void acc_mul_add(Acc& s, T d, T x)
@@ -267,6 +284,25 @@ struct PrecX
 		ff_prod(a.y, a.w, xih, xil, ih, il);
 		ff_acc_prod(ih, il, b.y, b.w, yih, yil);
 		return make_float4(rh, ih, rl, il);
+	}
+	// symmetric hop block: every output a 2-term compensated dot with coefficients (c, +-s);
+	// the string sign flips s (two sign bits), not the inputs
+	__device__ static void hop(T c0, T c1, unsigned sg, T& a, T& b)
+	{
+		const float ch = c0.x, cl = c0.z;
+		const float sh = __uint_as_float(__float_as_uint(c1.y) ^ (sg << 31)), sl = __uint_as_float(__float_as_uint(c1.w) ^ (sg << 31));
+		const T x = a, y = b;
+		float rh, rl, ih, il;
+		ff_prod(ch, cl, x.x, x.z, rh, rl);
+		ff_acc_prod(rh, rl, -sh, -sl, y.y, y.w);
+		ff_prod(ch, cl, x.y, x.w, ih, il);
+		ff_acc_prod(ih, il, sh, sl, y.x, y.z);
+		a = make_float4(rh, ih, rl, il);
+		ff_prod(ch, cl, y.x, y.z, rh, rl);
+		ff_acc_prod(rh, rl, -sh, -sl, x.y, x.w);
+		ff_prod(ch, cl, y.y, y.w, ih, il);
+		ff_acc_prod(ih, il, sh, sl, x.x, x.z);
+		b = make_float4(rh, ih, rl, il);
 	}
 	__device__ static Acc acc_zero() { return PrecF::acc_zero(); }
 	__device__ static void acc_mul_add(Acc& s, T d, T x)

@@ -31,6 +31,7 @@ namespace {
 constexpr int MAXKT = 14;   // at most 2^14 amplitudes per shared-memory tile
 constexpr int MAXNB = 31;   // compact bits (L <= 32)
 constexpr int MAXPM = 128;  // distinct gate matrices per target pass (staged in shared memory)
+constexpr int MAXPG = 128;  // gates per target pass (k_target_w stages their records in shared memory)
 
 struct PassRec
 {
@@ -182,6 +183,42 @@ void schedule(int L, int kt, const int* wires, int ng, bool reorder, Sched& s, i
 
 __device__ __forceinline__ unsigned ins0u(unsigned t, int p) { return ((t >> p) << (p + 1)) | (t & ((1u << p) - 1u)); }
 
+// shared-memory accesses by 32-bit shared-window address (ld/st.shared, no generic
+// addressing), for the state types of the precision policies
+__device__ __forceinline__ unsigned smem_u32(const void* p) { return (unsigned)__cvta_generic_to_shared(p); }
+template <class T> __device__ __forceinline__ T lds(unsigned a);
+template <class T> __device__ __forceinline__ void sts(unsigned a, const T& v);
+template <> __device__ __forceinline__ float4 lds<float4>(unsigned a)
+{
+	float4 v;
+	asm volatile("ld.shared.v4.f32 {%0, %1, %2, %3}, [%4];" : "=f"(v.x), "=f"(v.y), "=f"(v.z), "=f"(v.w) : "r"(a) : "memory");
+	return v;
+}
+template <> __device__ __forceinline__ void sts<float4>(unsigned a, const float4& v)
+{
+	asm volatile("st.shared.v4.f32 [%0], {%1, %2, %3, %4};" :: "r"(a), "f"(v.x), "f"(v.y), "f"(v.z), "f"(v.w) : "memory");
+}
+template <> __device__ __forceinline__ double2 lds<double2>(unsigned a)
+{
+	double2 v;
+	asm volatile("ld.shared.v2.f64 {%0, %1}, [%2];" : "=d"(v.x), "=d"(v.y) : "r"(a) : "memory");
+	return v;
+}
+template <> __device__ __forceinline__ void sts<double2>(unsigned a, const double2& v)
+{
+	asm volatile("st.shared.v2.f64 [%0], {%1, %2};" :: "r"(a), "d"(v.x), "d"(v.y) : "memory");
+}
+template <> __device__ __forceinline__ float2 lds<float2>(unsigned a)
+{
+	float2 v;
+	asm volatile("ld.shared.v2.f32 {%0, %1}, [%2];" : "=f"(v.x), "=f"(v.y) : "r"(a) : "memory");
+	return v;
+}
+template <> __device__ __forceinline__ void sts<float2>(unsigned a, const float2& v)
+{
+	asm volatile("st.shared.v2.f32 [%0], {%1, %2};" :: "r"(a), "f"(v.x), "f"(v.y) : "memory");
+}
+
 // Target gate record, precomputed on the host for a tile size and a block size
 // (all offsets in bytes of the swizzled tile):
 //   m   = { MW, MY, MZ, SCX }: a quartet's w, y, z slots are its x slot XOR MW, MY, MZ;
@@ -197,7 +234,9 @@ __device__ __forceinline__ unsigned ins0u(unsigned t, int p) { return ((t >> p) 
 // gate with a string has its off-diagonal entries negated on amplitudes whose string
 // bits have odd parity (a gate conjugated by the controlled-Z of a removed fermionic
 // swap).
-struct TGate { int4 m; int4 h; int d4, sl, snl, pad; };
+//   act = the range of rho (see k_target_w) whose quartets the gate changes:
+//         rho_min + 4 | (rho_max + 4) << 4 | 0x100 (0: the gate changes nothing)
+struct TGate { int4 m; int4 h; int d4, sl, snl, act; };
 
 struct ProgDev
 {
@@ -220,6 +259,7 @@ struct Args
 	const int2* upm;           // per target pass: offset into upmats (entries), matrix count
 	const T* upmats;           // per-pass distinct target matrices [8 entries each]
 	unsigned pm_off;           // byte offset of the staged matrices in shared memory
+	unsigned wperm_off;        // k_target_w: byte offset of the popcount-sorted free-bit table
 	int ngates;
 	const T* dense;            // -conj(U e_b) columns, or null (then U is run)
 	long dense_b0;
@@ -620,15 +660,16 @@ __host__ __device__ __forceinline__ unsigned tsw(unsigned e)
 // columns of equal parity sharing every index); SG: off-diagonal entries negated on the
 // pairs with sg[k] == 1 (implemented by negating the off-diagonal inputs)
 template <class P, int QPT, bool SG, int NC>
-__device__ __forceinline__ void tgt_block(char* tb, unsigned td, const unsigned (&x)[QPT], unsigned m0, unsigned m1, int kind,
-	unsigned rot, const typename P::T* m, const unsigned (&sg)[QPT])
+__device__ __forceinline__ void tgt_block(unsigned tb, unsigned td, const unsigned (&x)[QPT], unsigned m0, unsigned m1, int kind,
+	unsigned rot, unsigned m, const unsigned (&sg)[QPT])
 {
 	typedef typename P::T T;
 	T a[NC][QPT], b[NC][QPT];
-#define TGT_A(c, k) (*(T*)(tb + (c) * td + (x[k] ^ m0)))
-#define TGT_B(c, k) (*(T*)(tb + (c) * td + (x[k] ^ m1)))
-#define TGT_LOAD_AB() _Pragma("unroll") for (int c = 0; c < NC; c++) _Pragma("unroll") for (int k = 0; k < QPT; k++) { a[c][k] = TGT_A(c, k); b[c][k] = TGT_B(c, k); }
-#define TGT_LOAD_B() _Pragma("unroll") for (int c = 0; c < NC; c++) _Pragma("unroll") for (int k = 0; k < QPT; k++) b[c][k] = TGT_B(c, k);
+#define TGT_AA(c, k) (tb + (c) * td + (x[k] ^ m0))
+#define TGT_BA(c, k) (tb + (c) * td + (x[k] ^ m1))
+#define TGT_LOAD_AB() _Pragma("unroll") for (int c = 0; c < NC; c++) _Pragma("unroll") for (int k = 0; k < QPT; k++) { a[c][k] = lds<T>(TGT_AA(c, k)); b[c][k] = lds<T>(TGT_BA(c, k)); }
+#define TGT_LOAD_B() _Pragma("unroll") for (int c = 0; c < NC; c++) _Pragma("unroll") for (int k = 0; k < QPT; k++) b[c][k] = lds<T>(TGT_BA(c, k));
+#define TGT_MAT(q) lds<T>(m + (q) * (unsigned)sizeof(T))
 	switch (kind)
 	{
 	case BK_ID: return;
@@ -639,8 +680,8 @@ __device__ __forceinline__ void tgt_block(char* tb, unsigned td, const unsigned 
 #pragma unroll
 			for (int k = 0; k < QPT; k++)
 			{
-				TGT_A(c, k) = SG ? P::negif(b[c][k], sg[k]) : b[c][k];
-				TGT_B(c, k) = SG ? P::negif(a[c][k], sg[k]) : a[c][k];
+				sts<T>(TGT_AA(c, k), SG ? P::negif(b[c][k], sg[k]) : b[c][k]);
+				sts<T>(TGT_BA(c, k), SG ? P::negif(a[c][k], sg[k]) : a[c][k]);
 			}
 		return;
 	case BK_NEG1:
@@ -648,31 +689,31 @@ __device__ __forceinline__ void tgt_block(char* tb, unsigned td, const unsigned 
 #pragma unroll
 		for (int c = 0; c < NC; c++)
 #pragma unroll
-			for (int k = 0; k < QPT; k++) TGT_B(c, k) = P::neg(b[c][k]);
+			for (int k = 0; k < QPT; k++) sts<T>(TGT_BA(c, k), P::neg(b[c][k]));
 		return;
 	case BK_D1:
 	{
-		const T c3 = m[3];
+		const T c3 = TGT_MAT(3);
 		TGT_LOAD_B()
 #pragma unroll
 		for (int c = 0; c < NC; c++)
 #pragma unroll
-			for (int k = 0; k < QPT; k++) TGT_B(c, k) = P::mul(c3, b[c][k]);
+			for (int k = 0; k < QPT; k++) sts<T>(TGT_BA(c, k), P::mul(c3, b[c][k]));
 		return;
 	}
 	case BK_DIAG:
 	{
-		const T c0 = m[0], c3 = m[3];
+		const T c0 = TGT_MAT(0), c3 = TGT_MAT(3);
 		TGT_LOAD_AB()
 #pragma unroll
 		for (int c = 0; c < NC; c++)
 #pragma unroll
-			for (int k = 0; k < QPT; k++) { TGT_A(c, k) = P::mul(c0, a[c][k]); TGT_B(c, k) = P::mul(c3, b[c][k]); }
+			for (int k = 0; k < QPT; k++) { sts<T>(TGT_AA(c, k), P::mul(c0, a[c][k])); sts<T>(TGT_BA(c, k), P::mul(c3, b[c][k])); }
 		return;
 	}
 	case BK_ANTI:
 	{
-		const T c1 = m[1], c2 = m[2];
+		const T c1 = TGT_MAT(1), c2 = TGT_MAT(2);
 		TGT_LOAD_AB()
 #pragma unroll
 		for (int c = 0; c < NC; c++)
@@ -680,13 +721,13 @@ __device__ __forceinline__ void tgt_block(char* tb, unsigned td, const unsigned 
 			for (int k = 0; k < QPT; k++)
 			{
 				const T as = SG ? P::negif(a[c][k], sg[k]) : a[c][k], bs = SG ? P::negif(b[c][k], sg[k]) : b[c][k];
-				TGT_A(c, k) = P::mul(c1, bs); TGT_B(c, k) = P::mul(c2, as);
+				sts<T>(TGT_AA(c, k), P::mul(c1, bs)); sts<T>(TGT_BA(c, k), P::mul(c2, as));
 			}
 		return;
 	}
 	case BK_RI:
 	{
-		const T c0 = m[0], c1 = m[1], c2 = m[2], c3 = m[3];
+		const T c0 = TGT_MAT(0), c1 = TGT_MAT(1), c2 = TGT_MAT(2), c3 = TGT_MAT(3);
 		TGT_LOAD_AB()
 		if (rot == 6u)   // real diagonal, imaginary off-diagonal (hopping terms)
 		{
@@ -696,8 +737,8 @@ __device__ __forceinline__ void tgt_block(char* tb, unsigned td, const unsigned 
 				for (int k = 0; k < QPT; k++)
 				{
 					const T bs = SG ? P::negif(b[c][k], sg[k]) : b[c][k], as = SG ? P::negif(a[c][k], sg[k]) : a[c][k];
-					TGT_A(c, k) = P::madd2_ri(c0, false, a[c][k], c1, true, bs);
-					TGT_B(c, k) = P::madd2_ri(c2, true, as, c3, false, b[c][k]);
+					sts<T>(TGT_AA(c, k), P::madd2_ri(c0, false, a[c][k], c1, true, bs));
+					sts<T>(TGT_BA(c, k), P::madd2_ri(c2, true, as, c3, false, b[c][k]));
 				}
 		}
 		else
@@ -708,15 +749,15 @@ __device__ __forceinline__ void tgt_block(char* tb, unsigned td, const unsigned 
 				for (int k = 0; k < QPT; k++)
 				{
 					const T bs = SG ? P::negif(b[c][k], sg[k]) : b[c][k], as = SG ? P::negif(a[c][k], sg[k]) : a[c][k];
-					TGT_A(c, k) = P::madd2_ri(c0, rot & 1, a[c][k], c1, rot & 2, bs);
-					TGT_B(c, k) = P::madd2_ri(c2, rot & 4, as, c3, rot & 8, b[c][k]);
+					sts<T>(TGT_AA(c, k), P::madd2_ri(c0, rot & 1, a[c][k], c1, rot & 2, bs));
+					sts<T>(TGT_BA(c, k), P::madd2_ri(c2, rot & 4, as, c3, rot & 8, b[c][k]));
 				}
 		}
 		return;
 	}
 	default:
 	{
-		const T c0 = m[0], c1 = m[1], c2 = m[2], c3 = m[3];
+		const T c0 = TGT_MAT(0), c1 = TGT_MAT(1), c2 = TGT_MAT(2), c3 = TGT_MAT(3);
 		TGT_LOAD_AB()
 #pragma unroll
 		for (int c = 0; c < NC; c++)
@@ -724,21 +765,54 @@ __device__ __forceinline__ void tgt_block(char* tb, unsigned td, const unsigned 
 			for (int k = 0; k < QPT; k++)
 			{
 				const T bs = SG ? P::negif(b[c][k], sg[k]) : b[c][k], as = SG ? P::negif(a[c][k], sg[k]) : a[c][k];
-				TGT_A(c, k) = P::madd2(c0, a[c][k], c1, bs);
-				TGT_B(c, k) = P::madd2(c2, as, c3, b[c][k]);
+				sts<T>(TGT_AA(c, k), P::madd2(c0, a[c][k], c1, bs));
+				sts<T>(TGT_BA(c, k), P::madd2(c2, as, c3, b[c][k]));
 			}
 	}
 	}
-#undef TGT_A
-#undef TGT_B
+#undef TGT_AA
+#undef TGT_BA
 #undef TGT_LOAD_AB
 #undef TGT_LOAD_B
+#undef TGT_MAT
 }
+
+// a symmetric hop block [[c, i s], [i s, c]] on QPT pairs (slots x ^ m0, x ^ m1) of NC
+// tiles; SG: s negated on the pairs with sg[k] == 1 (a Jordan-Wigner string of odd parity)
+template <class P, int QPT, bool SG, int NC>
+__device__ __forceinline__ void tgt_hop(unsigned tb, unsigned td, const unsigned (&x)[QPT], unsigned m0, unsigned m1,
+	unsigned m, const unsigned (&sg)[QPT])
+{
+	typedef typename P::T T;
+	const T c0 = lds<T>(m), c1 = lds<T>(m + (unsigned)sizeof(T));
+	T a[NC][QPT], b[NC][QPT];
+#pragma unroll
+	for (int c = 0; c < NC; c++)
+#pragma unroll
+		for (int k = 0; k < QPT; k++)
+		{
+			a[c][k] = lds<T>(tb + c * td + (x[k] ^ m0));
+			b[c][k] = lds<T>(tb + c * td + (x[k] ^ m1));
+		}
+#pragma unroll
+	for (int c = 0; c < NC; c++)
+#pragma unroll
+		for (int k = 0; k < QPT; k++)
+		{
+			P::hop(c0, c1, SG ? sg[k] : 0u, a[c][k], b[c][k]);
+			sts<T>(tb + c * td + (x[k] ^ m0), a[c][k]);
+			sts<T>(tb + c * td + (x[k] ^ m1), b[c][k]);
+		}
+}
+
+// kind word of a gate (host classification): center kind | corner kind << 3 | center rot
+// << 6 | corner rot << 10 | symmetric-hop flags (center << 14, corner << 15)
+__device__ __forceinline__ bool kw_hop_center(int kw) { return (kw & 7) == 6 && ((kw >> 6) & 15) == 6 && ((kw >> 14) & 1); }
 
 // one target gate on the tile: QPT quartets per thread, q = t + k * blockDim.x
 // (QPT * blockDim.x == number of quartets); nlb: the tile's nonlocal compact bits
 template <class P, int QPT, int NC>
-__device__ __forceinline__ void tgt_gate(char* tb, unsigned td, const TGate& r, const typename P::T* mats, int tpar, unsigned nlb)
+__device__ __forceinline__ void tgt_gate(unsigned tb, unsigned td, const TGate& r, unsigned mats, int tpar, unsigned nlb)
 {
 	constexpr int ES = sizeof(typename P::T);
 	const unsigned MW = r.m.x, MY = r.m.y, MZ = r.m.z, SCX = r.m.w;
@@ -766,7 +840,7 @@ __device__ __forceinline__ void tgt_gate(char* tb, unsigned td, const TGate& r, 
 		}
 	}
 	const int kw = r.h.x >> 13;
-	const typename P::T* m = mats + (size_t)r.h.y * 8;
+	const unsigned m = mats + (unsigned)r.h.y * 8u * (unsigned)ES;   // the gate's staged matrix
 	unsigned sg[QPT];
 	if (r.sl | r.snl)
 	{
@@ -779,29 +853,31 @@ __device__ __forceinline__ void tgt_gate(char* tb, unsigned td, const TGate& r, 
 #pragma unroll
 		for (int k = 0; k < QPT; k++)
 			sg[k] = (s0 ^ ((k & 1) ? sp : 0u) ^ ((k & 2) ? (sp >> 1) : 0u) ^ ((k & 4) ? (sp >> 2) : 0u)) & 1u;
-		tgt_block<P, QPT, true, NC>(tb, td, x, 0u, MW, (kw >> 3) & 7, (kw >> 10) & 15, m + 4, sg);
+		tgt_block<P, QPT, true, NC>(tb, td, x, 0u, MW, (kw >> 3) & 7, (kw >> 10) & 15, m + 4 * ES, sg);
 #pragma unroll
 		for (int k = 0; k < QPT; k++) sg[k] ^= md;
-		tgt_block<P, QPT, true, NC>(tb, td, x, MY, MZ, kw & 7, (kw >> 6) & 15, m, sg);
+		if (kw_hop_center(kw)) tgt_hop<P, QPT, true, NC>(tb, td, x, MY, MZ, m, sg);
+		else tgt_block<P, QPT, true, NC>(tb, td, x, MY, MZ, kw & 7, (kw >> 6) & 15, m, sg);
 	}
 	else
 	{
-		tgt_block<P, QPT, false, NC>(tb, td, x, 0u, MW, (kw >> 3) & 7, (kw >> 10) & 15, m + 4, sg);
-		tgt_block<P, QPT, false, NC>(tb, td, x, MY, MZ, kw & 7, (kw >> 6) & 15, m, sg);
+		tgt_block<P, QPT, false, NC>(tb, td, x, 0u, MW, (kw >> 3) & 7, (kw >> 10) & 15, m + 4 * ES, sg);
+		if (kw_hop_center(kw)) tgt_hop<P, QPT, false, NC>(tb, td, x, MY, MZ, m, sg);
+		else tgt_block<P, QPT, false, NC>(tb, td, x, MY, MZ, kw & 7, (kw >> 6) & 15, m, sg);
 	}
 }
 
 // the same with one quartet per iteration, for tiles whose quartet count is not 4 or 8
 // times the block size
 template <class P, int NC>
-__device__ __forceinline__ void tgt_gate_any(char* tb, unsigned td, const TGate& r, const typename P::T* mats, int tpar, unsigned nlb,
+__device__ __forceinline__ void tgt_gate_any(unsigned tb, unsigned td, const TGate& r, unsigned mats, int tpar, unsigned nlb,
 	unsigned Q)
 {
 	constexpr int ES = sizeof(typename P::T);
 	const unsigned MW = r.m.x, MY = r.m.y, MZ = r.m.z, SCX = r.m.w;
 	const int lo = r.h.x & 31, hi = (r.h.x >> 5) & 31;
 	const int kw = r.h.x >> 13;
-	const typename P::T* m = mats + (size_t)r.h.y * 8;
+	const unsigned m = mats + (unsigned)r.h.y * 8u * (unsigned)ES;
 	const unsigned ml = (unsigned)r.sl & 0xffffu, md = ((unsigned)r.sl >> 16) & 1u;
 	const unsigned sn = (unsigned)__popc(nlb & (unsigned)r.snl);
 	for (unsigned q = threadIdx.x; q < Q; q += blockDim.x)
@@ -811,14 +887,14 @@ __device__ __forceinline__ void tgt_gate_any(char* tb, unsigned td, const TGate&
 		const unsigned x[1] = { (tsw<ES>(e) * ES) ^ (pe ? SCX : 0u) };
 		const unsigned sgk[1] = { ((unsigned)__popc(e & ml) + sn + (md ? pe : 0u)) & 1u };
 		const unsigned sgc[1] = { sgk[0] ^ md };
-		tgt_block<P, 1, true, NC>(tb, td, x, 0u, MW, (kw >> 3) & 7, (kw >> 10) & 15, m + 4, sgk);
+		tgt_block<P, 1, true, NC>(tb, td, x, 0u, MW, (kw >> 3) & 7, (kw >> 10) & 15, m + 4 * ES, sgk);
 		tgt_block<P, 1, true, NC>(tb, td, x, MY, MZ, kw & 7, (kw >> 6) & 15, m, sgc);
 	}
 }
 
 // the gates [gbeg, gend) of a pass on one tile, records read one gate ahead
 template <class P, int QPT, int NC>
-__device__ __forceinline__ void tgt_gates(char* tb, unsigned td, const TGate* gates, int gbeg, int gend, const typename P::T* mats,
+__device__ __forceinline__ void tgt_gates(unsigned tb, unsigned td, const TGate* gates, int gbeg, int gend, unsigned mats,
 	int tpar, unsigned nlb, unsigned Q)
 {
 	if (gbeg >= gend) return;
@@ -833,10 +909,116 @@ __device__ __forceinline__ void tgt_gates(char* tb, unsigned td, const TGate* ga
 	}
 }
 
+// ------------------------------------------------------------------------------------
+// Weight-restricted target sweep (k_target_w), for targets whose every gate conserves the
+// Hamming weight (corner blocks diagonal: hopping and interaction terms of particle-
+// conserving Hamiltonians, fermionic swaps).  U e_b then lives on the amplitudes of weight
+// |b|: compact indices c (qubit L-1 dropped) with popc(c) in {|b| - 1, |b|}.  The members
+// of a gate's quartet have popcounts r + (0, 1, 1, 2) in some order (r: popcount of the
+// quartet's free bits, the tile's nonlocal bits adding popc(nlb)), so whether a quartet
+// holds a nonzero amplitude that the gate changes depends only on
+// rho = r - (|b| - popc(nlb)), in [-3, 0]; the host stores that range per gate (TGate.act).
+// The quartets of a range of r are one run of the free-bit values sorted by popcount (a
+// table in shared memory), so each gate's live quartets are enumerated without divergence.
+// The skipped quartets hold zeros the gate maps to zeros: results are bit-identical to
+// the full sweep.
+// ------------------------------------------------------------------------------------
+
+// byte offset of the popcount starts after the sorted free-bit table (16-byte aligned)
+__host__ __device__ constexpr unsigned wtab_start_off(int kt) { return ((2u << (kt - 2)) + 15u) & ~15u; }
+// byte offset of the staged gate records of a pass (after 16 popcount starts)
+__host__ __device__ constexpr unsigned wtab_rec_off(int kt) { return wtab_start_off(kt) + 16u * (unsigned)sizeof(int); }
+
+// the free-bit values 0 .. 2^F - 1 sorted by popcount (ties by value) into perm, and
+// start[r] = index of the first value of popcount r (start[F + 1] = 2^F); whole block
+__device__ __forceinline__ void w_perm_setup(int F, unsigned short* perm, int* start)
+{
+	auto binom = [](int n, int k) {
+		if (k < 0 || k > n) return 0;
+		int c = 1;
+		for (int i = 0; i < k; i++) c = c * (n - i) / (i + 1);
+		return c;
+	};
+	const unsigned nq = 1u << F;
+	for (unsigned v = threadIdx.x; v < nq; v += blockDim.x)
+	{
+		// rank among the values of the same popcount (combinatorial number system)
+		int rank = 0, i = 0;
+		for (int p = 0; p < F; p++)
+			if (v & (1u << p)) rank += binom(p, ++i);
+		int off = 0;
+		for (int r = 0; r < i; r++) off += binom(F, r);
+		perm[off + rank] = (unsigned short)v;
+	}
+	for (int r = threadIdx.x; r <= F + 1; r += blockDim.x)
+	{
+		int off = 0;
+		for (int q = 0; q < r; q++) off += binom(F, q);
+		start[r] = off;
+	}
+}
+
+// NQ live quartets of a gate: the ones at popcount-sorted positions j + k * stride
+template <class P, int NQ, bool SG>
+__device__ __forceinline__ void tgt_quartets_w(unsigned tb, unsigned td, const TGate& r, unsigned m, int tpar, unsigned sn,
+	const unsigned short* perm, unsigned j, unsigned stride)
+{
+	constexpr int ES = sizeof(typename P::T);
+	const int lo = r.h.x & 31, hi = (r.h.x >> 5) & 31, kw = r.h.x >> 13;
+	const unsigned SCX = r.m.w, ml = (unsigned)r.sl & 0xffffu, md = ((unsigned)r.sl >> 16) & 1u;
+	unsigned x[NQ], sg[NQ];
+#pragma unroll
+	for (int k = 0; k < NQ; k++)
+	{
+		const unsigned e = ins0u(ins0u(perm[j + k * stride], lo), hi);
+		const unsigned pe = (unsigned)(__popc(e) + tpar) & 1u;
+		x[k] = (tsw<ES>(e) * ES) ^ (pe ? SCX : 0u);
+		sg[k] = SG ? (((unsigned)__popc(e & ml) + sn + (md ? pe : 0u)) & 1u) : 0u;
+	}
+	tgt_block<P, NQ, SG, 1>(tb, td, x, 0u, (unsigned)r.m.x, (kw >> 3) & 7, (kw >> 10) & 15, m + 4 * ES, sg);
+	if (SG)
+#pragma unroll
+		for (int k = 0; k < NQ; k++) sg[k] ^= md;
+	if (kw_hop_center(kw)) tgt_hop<P, NQ, SG, 1>(tb, td, x, (unsigned)r.m.y, (unsigned)r.m.z, m, sg);
+	else tgt_block<P, NQ, SG, 1>(tb, td, x, (unsigned)r.m.y, (unsigned)r.m.z, kw & 7, (kw >> 6) & 15, m, sg);
+}
+
+// one gate on the live quartets [j0, j1) of the popcount-sorted order, two per iteration
+template <class P, bool SG>
+__device__ __forceinline__ void tgt_gate_w(unsigned tb, unsigned td, const TGate& r, unsigned mats, int tpar, unsigned nlb,
+	const unsigned short* perm, unsigned j0, unsigned j1)
+{
+	constexpr int ES = sizeof(typename P::T);
+	const unsigned m = mats + (unsigned)r.h.y * 8u * (unsigned)ES;
+	const unsigned sn = SG ? (unsigned)__popc(nlb & (unsigned)r.snl) : 0u;
+	unsigned j = j0 + threadIdx.x;
+	for (; j + blockDim.x < j1; j += 2 * blockDim.x) tgt_quartets_w<P, 2, SG>(tb, td, r, m, tpar, sn, perm, j, blockDim.x);
+	if (j < j1) tgt_quartets_w<P, 1, SG>(tb, td, r, m, tpar, sn, perm, j, blockDim.x);
+}
+
+// the gates [gbeg, gend) of a pass on one tile of nonlocal bits nlb, for a column of weight
+// wb; F free bits per quartet.  One barrier per gate that has live quartets in the tile.
+template <class P>
+__device__ __forceinline__ void tgt_gates_w(unsigned tb, unsigned td, const TGate* gates, int gbeg, int gend, unsigned mats,
+	int tpar, unsigned nlb, int wb, int F, const unsigned short* perm, const int* start)
+{
+	const int delta = wb - __popc(nlb);
+	for (int gi = gbeg; gi < gend; gi++)
+	{
+		const TGate r = gates[gi];
+		if (!(r.act & 0x100)) continue;
+		const int rlo = max(0, delta + (r.act & 15) - 4), rhi = min(F, delta + ((r.act >> 4) & 15) - 4);
+		if (rlo > rhi) continue;   // no live quartet in this tile (the same for the whole block)
+		if (r.sl | r.snl) tgt_gate_w<P, true>(tb, td, r, mats, tpar, nlb, perm, (unsigned)start[rlo], (unsigned)start[rhi + 1]);
+		else tgt_gate_w<P, false>(tb, td, r, mats, tpar, nlb, perm, (unsigned)start[rlo], (unsigned)start[rhi + 1]);
+		__syncthreads();
+	}
+}
+
 // -conj(U e_b) of NC basis columns bs (of equal parity) into outs (the whole block); QPT:
 // quartets per thread and gate (0: any, one quartet per iteration).  Shared memory: NC
 // tiles, then the deposit tables and scratch; the pass matrices at a.pm_off.
-template <class P, int QPT, int NC>
+template <class P, int QPT, int NC, bool W = false>
 __device__ __forceinline__ void tgt_column(const Args<P>& a, const long (&bs)[NC], typename P::T* const (&outs)[NC], char* smem_raw)
 {
 	typedef typename P::T T;
@@ -845,8 +1027,9 @@ __device__ __forceinline__ void tgt_column(const Args<P>& a, const long (&bs)[NC
 	const unsigned n = 1u << kt, Q = n >> 2, td = n * ES;
 	T* tile_last;
 	Smem s = smem_layout<T>(smem_raw + (NC - 1) * td, kt, tile_last);
-	char* tb = smem_raw;
+	const unsigned tb = smem_u32(smem_raw);                 // the tiles, by shared-window address
 	T* pm = reinterpret_cast<T*>(smem_raw + a.pm_off);   // this pass's distinct matrices
+	const unsigned pms = smem_u32(pm);
 	const int par = __popcll(bs[0]) & 1;
 	for (int p = 0; p < a.U.npass; p++)
 	{
@@ -856,6 +1039,14 @@ __device__ __forceinline__ void tgt_column(const Args<P>& a, const long (&bs)[NC
 		{
 			const int2 mp = a.upm[p];
 			for (int i = threadIdx.x; i < mp.y * 8; i += blockDim.x) pm[i] = a.upmats[mp.x + i];
+		}
+		if (W)
+		{
+			// this pass's gate records, read by every tile of the pass
+			const int4* src = reinterpret_cast<const int4*>(a.utg + pr.gbeg);
+			int4* dst = reinterpret_cast<int4*>(smem_raw + a.wperm_off + wtab_rec_off(kt));
+			const int n4 = (pr.gend - pr.gbeg) * (int)(sizeof(TGate) / sizeof(int4));
+			for (int i = threadIdx.x; i < n4; i += blockDim.x) dst[i] = src[i];
 		}
 		__syncthreads();
 		const bool last = p == a.U.npass - 1;
@@ -867,13 +1058,13 @@ __device__ __forceinline__ void tgt_column(const Args<P>& a, const long (&bs)[NC
 #pragma unroll
 			for (int c = 0; c < NC; c++)
 			{
-				T* tile = reinterpret_cast<T*>(tb + c * td);
+				const unsigned tile = tb + c * td;
 				const T* out = outs[c];
 				if (p == 0)
 				{
 					const unsigned cb = (unsigned)(bs[c] >> 1);
 					for (unsigned e = threadIdx.x; e < n; e += blockDim.x)
-						tile[tsw<ES>(e)] = (gidx(s, nlb, e) == cb) ? P::make(1.0, 0.0) : P::zero();
+						sts<T>(tile + tsw<ES>(e) * ES, (gidx(s, nlb, e) == cb) ? P::make(1.0, 0.0) : P::zero());
 				}
 				else
 					for (unsigned e0 = threadIdx.x; e0 < n; e0 += 8 * blockDim.x)
@@ -889,20 +1080,25 @@ __device__ __forceinline__ void tgt_column(const Args<P>& a, const long (&bs)[NC
 						for (int k = 0; k < 8; k++)
 						{
 							const unsigned e = e0 + k * blockDim.x;
-							if (e < n) tile[tsw<ES>(e)] = v[k];
+							if (e < n) sts<T>(tile + tsw<ES>(e) * ES, v[k]);
 						}
 					}
 			}
 			__syncthreads();
-			tgt_gates<P, QPT, NC>(tb, td, a.utg, pr.gbeg, pr.gend, pm, tpar, nlb, Q);
+			if (W)
+				tgt_gates_w<P>(tb, td, reinterpret_cast<const TGate*>(smem_raw + a.wperm_off + wtab_rec_off(kt)), 0,
+					pr.gend - pr.gbeg, pms, tpar, nlb, __popcll(bs[0]), kt - 2,
+					reinterpret_cast<const unsigned short*>(smem_raw + a.wperm_off),
+					reinterpret_cast<const int*>(smem_raw + a.wperm_off + wtab_start_off(kt)));
+			else tgt_gates<P, QPT, NC>(tb, td, a.utg, pr.gbeg, pr.gend, pms, tpar, nlb, Q);
 #pragma unroll
 			for (int c = 0; c < NC; c++)
 			{
-				const T* tile = reinterpret_cast<const T*>(tb + c * td);
+				const unsigned tile = tb + c * td;
 				T* out = outs[c];
 				for (unsigned e = threadIdx.x; e < n; e += blockDim.x)
 				{
-					const T v = tile[tsw<ES>(e)];
+					const T v = lds<T>(tile + tsw<ES>(e) * ES);
 					out[gidx(s, nlb, e)] = last ? P::negconj(v) : v;
 				}
 			}
@@ -922,12 +1118,33 @@ __device__ __forceinline__ void tgt_column(const Args<P>& a, long b, typename P:
 // one instantiation per (block size, quartets per thread), so that each keeps only its
 // own path's registers: 256 threads with 4, 8 or any quartets; 512 with 2, 4 or any
 template <class P, int NT, int QPT>
-__global__ void __launch_bounds__(NT, (NT == 512 && QPT == 4) ? 1 : 2) k_target(Args<P> a)
+__global__ void __launch_bounds__(NT, (NT == 512 && QPT == 4) ? 1 : (NT == 128 ? 3 : 2)) k_target(Args<P> a)
 {
 	extern __shared__ __align__(16) char smem_raw[];
 	for (long b = a.b0 + blockIdx.x; b < a.b1; b += gridDim.x)
 		tgt_column<P, QPT>(a, b, a.ucols + (size_t)(b - a.b0) * a.S, smem_raw);
 }
+
+// the weight-restricted sweep (targets that conserve the Hamming weight), 128 threads
+template <class P>
+__global__ void __launch_bounds__(128, 3) k_target_w(Args<P> a)
+{
+	extern __shared__ __align__(16) char smem_raw[];
+	w_perm_setup(a.kt - 2, reinterpret_cast<unsigned short*>(smem_raw + a.wperm_off),
+		reinterpret_cast<int*>(smem_raw + a.wperm_off + wtab_start_off(a.kt)));
+	for (long b = a.b0 + blockIdx.x; b < a.b1; b += gridDim.x)
+	{
+		const long bs[1] = { b };
+		typename P::T* const outs[1] = { a.ucols + (size_t)(b - a.b0) * a.S };
+		tgt_column<P, 0, 1, true>(a, bs, outs, smem_raw);
+	}
+}
+
+// bytes of k_target_w's tables after the staged matrices: the sorted free-bit values and
+// the popcount starts
+// bytes of k_target_w's tables after the staged matrices: the sorted free-bit values, the
+// popcount starts and the records of one pass (at most maxg gates)
+constexpr size_t wtab_bytes(int kt, int maxg) { return wtab_rec_off(kt) + (size_t)maxg * sizeof(TGate); }
 
 // two columns of equal parity per block (b, b ^ 3 within each aligned group of four),
 // sharing every per-gate computation; columns outside whole groups one at a time
@@ -963,6 +1180,7 @@ static void (*target_kernel(int kt, int threads, int nc = 1))(Args<P>)
 	const long q = (1L << (kt - 2)) / threads, exact = (1L << (kt - 2)) % threads == 0;
 	if (nc == 2) return (exact && q == 4) ? k_target2<P, 4> : (exact && q == 8) ? k_target2<P, 8> : k_target2<P, 0>;
 	if (threads > 256) return (exact && q == 2) ? k_target<P, 512, 2> : (exact && q == 4) ? k_target<P, 512, 4> : k_target<P, 512, 0>;
+	if (threads == 128 && exact && q == 8) return k_target<P, 128, 8>;
 	if (exact && q == 4) return k_target<P, 256, 4>;
 	if (exact && q == 8) return k_target<P, 256, 8>;
 	return k_target<P, 256, 0>;
@@ -1436,6 +1654,9 @@ int grid_cap(long work, int threads)
 struct TargetProg
 {
 	int kt = -1, prec = -1, threads = -1;
+	int max_pm = MAXPM;            // most distinct matrices any pass stages
+	bool wcons = false;            // every gate conserves the Hamming weight (k_target_w applies)
+	int max_g = MAXPG;             // most gates in one pass
 	Sched sched;
 	DevBuf pass, gate, mats, kinds, tg, pm, pmats;
 };
@@ -1466,6 +1687,13 @@ static int classify_block(const mgc* e, unsigned& rot, mgc* stored)
 	return BK_RI;
 }
 
+// 1 for a block [[c, i s], [i s, c]] with c, s real (a hopping term): BK_RI with real
+// diagonal and imaginary off-diagonal entries, equal in pairs
+static int sym_hop(int kind, unsigned rot, const mgc* e)
+{
+	return kind == BK_RI && rot == 6u && e[0].re == e[3].re && e[1].im == e[2].im;
+}
+
 template <class P>
 static int upload_target_mats(const mgg* gates, int ng, DevBuf& buf, DevBuf& kinds, std::vector<int>& k)
 {
@@ -1477,7 +1705,8 @@ static int upload_target_mats(const mgg* gates, int ng, DevBuf& buf, DevBuf& kin
 		mgc sc[4], sk[4];
 		unsigned rc, rk;
 		const int kc = classify_block(gates[g].c, rc, sc), kk = classify_block(gates[g].k, rk, sk);
-		k[g] = kc | (kk << 3) | (int)(rc << 6) | (int)(rk << 10);
+		k[g] = kc | (kk << 3) | (int)(rc << 6) | (int)(rk << 10) | (sym_hop(kc, rc, gates[g].c) << 14)
+			| (sym_hop(kk, rk, gates[g].k) << 15);
 		for (int q = 0; q < 4; q++)
 		{
 			h[(size_t)g * 8 + q] = P::make(sc[q].re, sc[q].im);
@@ -1624,6 +1853,32 @@ static int upload_sched(const Sched& s, DevBuf& pass, DevBuf& gate)
 	return 0;
 }
 
+// TGate.act of a gate (type as in GateRec, kinds of its center and corner block): the
+// range of rho = r - (|b| - popc(nlb)) for which the gate changes a nonzero amplitude of a
+// column of weight |b|.  A member of popcount offset o (over r) is nonzero when
+// rho + o is -1 or 0; gates on the dropped qubit pair their members by the parity of the
+// quartet's base, which equals the parity of rho.
+static int weight_act(int type, int kc, int kk)
+{
+	auto live = [](int rho, int o) { return rho + o == -1 || rho + o == 0; };
+	auto changes = [&](int kind, int rho, int oa, int ob) {
+		if (kind == BK_ID) return false;
+		if (kind == BK_D1 || kind == BK_NEG1) return live(rho, ob);   // only the second member moves
+		return live(rho, oa) || live(rho, ob);
+	};
+	int lo = 99, hi = -99;
+	for (int rho = -3; rho <= 0; rho++)
+	{
+		const int sp = rho & 1;
+		int ox, ow, oy, oz;   // popcount offsets of x, w (corner pair) and y, z (center pair)
+		if (type == 0) { ox = 0; ow = 2; oy = 1; oz = 1; }
+		else if (type == 1) { if (!sp) { ox = 0; ow = 1; oy = 1; oz = 2; } else { ox = 1; ow = 2; oy = 0; oz = 1; } }
+		else { if (!sp) { ox = 0; ow = 1; oy = 2; oz = 1; } else { ox = 1; ow = 2; oy = 1; oz = 0; } }
+		if (changes(kk, rho, ox, ow) || changes(kc, rho, oy, oz)) { lo = std::min(lo, rho); hi = std::max(hi, rho); }
+	}
+	return lo <= hi ? (0x100 | (lo + 4) | (hi + 4) << 4) : 0;
+}
+
 template <class P>
 static int build_target_prog(mgcu_target* t, int kt, int threads, TargetProg& tp)
 {
@@ -1660,7 +1915,7 @@ static int build_target_prog(mgcu_target* t, int kt, int threads, TargetProg& tp
 					std::map<int, int> loc;
 					const int off = (int)pm_first.size();
 					int ge = gb;
-					for (; ge < pr.gend; ge++)
+					for (; ge < pr.gend && ge - gb < MAXPG; ge++)
 					{
 						const int u = uid[tp.sched.gate[ge].g];
 						auto it = loc.find(u);
@@ -1682,6 +1937,10 @@ static int build_target_prog(mgcu_target* t, int kt, int threads, TargetProg& tp
 			}
 			tp.sched.pass.swap(split.pass);
 		}
+		tp.max_pm = 1;
+		for (const int2& v : pmh) tp.max_pm = std::max(tp.max_pm, v.y);
+		tp.max_g = 1;
+		for (const PassRec& q : tp.sched.pass) tp.max_g = std::max(tp.max_g, q.gend - q.gbeg);
 		int e = upload_sched(tp.sched, tp.pass, tp.gate);
 		if (e) return e;
 		std::vector<int> kw;
@@ -1744,6 +2003,14 @@ static int build_target_prog(mgcu_target* t, int kt, int threads, TargetProg& tp
 			o.h.z = (int)d[0]; o.h.w = (int)d[1]; o.d4 = (int)d[2];
 			o.sl = (int)(ml | md << 16 | spar << 17);
 			o.snl = (int)mnl;
+			o.act = weight_act(r.type, kw[r.g] & 7, (kw[r.g] >> 3) & 7);
+		}
+		// the weight-restricted sweep applies when no corner block mixes |00> and |11>
+		tp.wcons = true;
+		for (size_t i = 0; i < tp.sched.gate.size(); i++)
+		{
+			const int kk = (kw[tp.sched.gate[i].g] >> 3) & 7;
+			tp.wcons = tp.wcons && (kk == BK_ID || kk == BK_D1 || kk == BK_NEG1 || kk == BK_DIAG);
 		}
 		e = tp.tg.alloc(sizeof(TGate) * tg.size());
 		if (e) return e;
@@ -1787,6 +2054,15 @@ static int target_prog(mgcu_target* t, int kt, int threads, TargetProg*& out)
 	return 0;
 }
 
+template <class P>
+static int target_pm_cap(mgcu_target* t, int kt, int threads, int& cap, bool& wcons, int& maxg)
+{
+	TargetProg* tp = nullptr;
+	const int e = target_prog<P>(t, kt, threads, tp);
+	if (!e) { cap = tp->max_pm; wcons = tp->wcons; maxg = tp->max_g; }
+	return e;
+}
+
 extern "C" mgcu_target* mgcu_target_circuit(const mgg* gates, const int* wires, int ngates, int L)
 {
 	if (!mgcu_ctx()) return nullptr;
@@ -1820,6 +2096,22 @@ extern "C" int mgcu_target_sweep_gates(mgcu_target* t)
 	prepare_sweep(t);
 	return (int)t->sg.size();
 }
+
+// 1 when every gate of the swept circuit conserves the Hamming weight (no corner block
+// mixes |00> and |11>), so the GPU sweep visits only the amplitudes of the column's weight
+extern "C" int mgcu_target_conserves_weight(mgcu_target* t)
+{
+	if (t->kind != 0) return 0;
+	prepare_sweep(t);
+	for (const mgg& g : t->sg)
+	{
+		unsigned rot;
+		mgc st[4];
+		const int kk = classify_block(g.k, rot, st);
+		if (kk != BK_ID && kk != BK_D1 && kk != BK_NEG1 && kk != BK_DIAG) return 0;
+	}
+	return 1;
+}
 extern "C" int mgcu_target_L(const mgcu_target* t) { return t->L; }
 extern "C" void mgcu_target_set_resident(mgcu_target* t, int enable)
 {
@@ -1846,7 +2138,10 @@ struct mgcu_plan
 	std::vector<double> place_w;
 	int L, nb, kt, threads, grid_a, grid_b, grid_t, prec;
 	int kt_t, threads_t, nc_t;     // k_target's tile bits, block size and columns per block
-	size_t smem_t;                 // k_target: its tile, tables, scratch and MAXPM staged matrices
+	size_t smem_t;                 // k_target: its tile, tables, scratch and pm_cap staged matrices
+	int pm_cap = MAXPM;            // staged matrices per pass k_target has room for
+	bool w_t = false;              // the weight-restricted sweep (k_target_w)
+	int maxg_t = MAXPG;            // k_target_w: room for this many staged gate records
 	bool ktime = false;            // record events around k_target launches (mgcu_plan_time_ms)
 	std::vector<cudaEvent_t> kev;  // start/stop pairs
 	size_t kev_used = 0;
@@ -1881,7 +2176,11 @@ static int launch_target(mgcu_plan* p, long b0, long b1, typename P::T* out)
 	a.utg = tp->tg.as<TGate>();
 	a.upm = tp->pm.as<int2>();
 	a.upmats = tp->pmats.as<T>();
-	a.pm_off = (unsigned)(p->smem_t - (size_t)MAXPM * 8 * p->tsize);
+	if (tp->max_pm > p->pm_cap) { mg_set_error("target program stages %d matrices per pass, room for %d", tp->max_pm, p->pm_cap); return MG_ERR_ARG; }
+	if (p->w_t && tp->max_g > p->maxg_t) { mg_set_error("target pass has %d gates, room for %d", tp->max_g, p->maxg_t); return MG_ERR_ARG; }
+	const size_t wtab = p->w_t ? wtab_bytes(p->kt_t, p->maxg_t) : 0;
+	a.pm_off = (unsigned)(p->smem_t - wtab - (size_t)p->pm_cap * 8 * p->tsize);
+	a.wperm_off = (unsigned)(p->smem_t - wtab);
 	a.b0 = b0; a.b1 = b1;
 	a.ucols = out;
 	const int grid = (int)std::min<long>(p->grid_t, p->nc_t == 2 ? std::max(1L, (b1 - b0 + 1) / 2) : b1 - b0);
@@ -1893,7 +2192,7 @@ static int launch_target(mgcu_plan* p, long b0, long b1, typename P::T* out)
 			p->kev.push_back(ev);
 		}
 	if (p->ktime) MGCU_TRY(cudaEventRecord(p->kev[p->kev_used], c->stream));
-	void (*kern)(Args<P>) = target_kernel<P>(p->kt_t, p->threads_t, p->nc_t);
+	void (*kern)(Args<P>) = p->w_t ? k_target_w<P> : target_kernel<P>(p->kt_t, p->threads_t, p->nc_t);
 	if (!kern) { mg_set_error("no target-sweep kernel for 2^%d amplitudes and %d threads", p->kt_t, p->threads_t); return MG_ERR_ARG; }
 	kern<<<grid, p->threads_t, p->smem_t, c->stream>>>(a);
 	MGCU_LAUNCHED();
@@ -1945,20 +2244,21 @@ static int set_smem_attr()
 {
 	MgcuContext* c = mgcu_ctx();
 	MGCU_TRY(cudaFuncSetAttribute(k_columns<P, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)std::min<size_t>(c->smem_optin, 227 * 1024)));
-	void (*const tk[9])(Args<P>) = { k_target<P, 256, 4>, k_target<P, 256, 8>, k_target<P, 256, 0>, k_target<P, 512, 2>,
-		k_target<P, 512, 4>, k_target<P, 512, 0>, k_target2<P, 4>, k_target2<P, 8>, k_target2<P, 0> };
+	void (*const tk[10])(Args<P>) = { k_target<P, 256, 4>, k_target<P, 256, 8>, k_target<P, 256, 0>, k_target<P, 512, 2>,
+		k_target<P, 512, 4>, k_target<P, 512, 0>, k_target2<P, 4>, k_target2<P, 8>, k_target2<P, 0>, k_target<P, 128, 8> };
 	for (auto k : tk) MGCU_TRY(cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)std::min<size_t>(c->smem_optin, 227 * 1024)));
+	MGCU_TRY(cudaFuncSetAttribute(k_target_w<P>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)std::min<size_t>(c->smem_optin, 227 * 1024)));
 	MGCU_TRY(cudaFuncSetAttribute(k_hessian<P>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)std::min<size_t>(c->smem_optin, 227 * 1024)));
 	return 0;
 }
 
 template <class P>
-static int occupancy(int threads, size_t smem, int kt_t, int threads_t, int nc_t, size_t smem_t, int& per_sm, int& per_sm_target)
+static int occupancy(int threads, size_t smem, int kt_t, int threads_t, int nc_t, size_t smem_t, bool w_t, int& per_sm, int& per_sm_target)
 {
 	int n1 = 0, n2 = 0, n3 = 0;
 	MGCU_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n1, k_columns<P, false>, threads, smem));
 	MGCU_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n2, k_hessian<P>, threads, smem));
-	void (*kern)(Args<P>) = target_kernel<P>(kt_t, threads_t, nc_t);
+	void (*kern)(Args<P>) = w_t ? k_target_w<P> : target_kernel<P>(kt_t, threads_t, nc_t);
 	if (!kern) { mg_set_error("no target-sweep kernel for 2^%d amplitudes and %d threads", kt_t, threads_t); return MG_ERR_ARG; }
 	MGCU_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n3, kern, threads_t, smem_t));
 	per_sm = std::max(1, std::min(n1, n2));
@@ -2021,18 +2321,45 @@ extern "C" mgcu_plan* mgcu_plan_create(const mgcu_plan_desc* d)
 		if (o > 0) ktt = (int)std::max(5L, std::min<long>(o, MAXKT));
 		while (ktt > 5 && ((size_t)1 << ktt) * p->tsize > 128 * 1024) ktt--;
 		p->kt_t = std::min(ktt, p->nb);
+		// 2^12 amplitudes of 16 B: 128 threads with eight quartets each, three blocks per SM
+		// (measured at L=16: 0.460 s per 8192-column launch against 0.495 s with 256 x 4)
 		int tt = std::max(32, std::min(256, 1 << (p->kt_t - 2)));
+		if (p->tsize == 16 && p->kt_t == 12) tt = 128;
 		const long ot = mgcu_option(MG_OPT_TARGET_THREADS_ID);
 		if (ot > 0) tt = (int)std::max(32L, std::min(512L, (ot / 32) * 32));
 		p->threads_t = tt;
 		p->nc_t = (mgcu_option(MG_OPT_TARGET_COLUMNS_ID) == 2 && tt == 256) ? 2 : 1;
+		// targets that conserve the Hamming weight run the weight-restricted sweep (128
+		// threads, one column per block) unless TARGET_DENSE asks for the full one
+		bool wcons = false;
+		if (d->target && d->target->kind == 0 && p->nc_t == 1 && mgcu_option(MG_OPT_TARGET_DENSE_ID) == 0
+			&& (ot <= 0 || tt == 128))
+		{
+			int e = 0, mp = MAXPM, mg = MAXPG;
+			if (p->prec == MG_PREC_FP64_ID) e = target_pm_cap<PrecD>(d->target, p->kt_t, 128, mp, wcons, mg);
+			else if (p->prec == MG_PREC_FP32_ID) e = target_pm_cap<PrecF>(d->target, p->kt_t, 128, mp, wcons, mg);
+			else e = target_pm_cap<PrecX>(d->target, p->kt_t, 128, mp, wcons, mg);
+			if (e) { delete p; return nullptr; }
+			if (wcons) { p->threads_t = tt = 128; p->pm_cap = mp; p->w_t = true; p->maxg_t = mg; }
+		}
+		// room for the staged matrices of the target's busiest pass (built here, cached on the target)
+		if (d->target && d->target->kind == 0 && !p->w_t)
+		{
+			int e = 0, mp = MAXPM, mg = MAXPG;
+			if (p->prec == MG_PREC_FP64_ID) e = target_pm_cap<PrecD>(d->target, p->kt_t, tt, mp, wcons, mg);
+			else if (p->prec == MG_PREC_FP32_ID) e = target_pm_cap<PrecF>(d->target, p->kt_t, tt, mp, wcons, mg);
+			else e = target_pm_cap<PrecX>(d->target, p->kt_t, tt, mp, wcons, mg);
+			if (e) { delete p; return nullptr; }
+			p->pm_cap = mp;
+		}
 		p->smem_t = (size_t)p->nc_t * ((size_t)1 << p->kt_t) * p->tsize + 2 * 128 * sizeof(unsigned)
-			+ std::max<size_t>((size_t)(tt / 32) * 16 * sizeof(double), 16 * 16) + (size_t)MAXPM * 8 * p->tsize;
+			+ std::max<size_t>((size_t)(tt / 32) * 16 * sizeof(double), 16 * 16) + (size_t)p->pm_cap * 8 * p->tsize
+			+ (p->w_t ? wtab_bytes(p->kt_t, p->maxg_t) : 0);
 	}
 	int per_sm = 1, per_sm_t = 1, e = 0;
-	if (p->prec == MG_PREC_FP64_ID) { e = set_smem_attr<PrecD>(); if (!e) e = occupancy<PrecD>(threads, p->smem, p->kt_t, p->threads_t, p->nc_t, p->smem_t, per_sm, per_sm_t); }
-	else if (p->prec == MG_PREC_FP32_ID) { e = set_smem_attr<PrecF>(); if (!e) e = occupancy<PrecF>(threads, p->smem, p->kt_t, p->threads_t, p->nc_t, p->smem_t, per_sm, per_sm_t); }
-	else { e = set_smem_attr<PrecX>(); if (!e) e = occupancy<PrecX>(threads, p->smem, p->kt_t, p->threads_t, p->nc_t, p->smem_t, per_sm, per_sm_t); }
+	if (p->prec == MG_PREC_FP64_ID) { e = set_smem_attr<PrecD>(); if (!e) e = occupancy<PrecD>(threads, p->smem, p->kt_t, p->threads_t, p->nc_t, p->smem_t, p->w_t, per_sm, per_sm_t); }
+	else if (p->prec == MG_PREC_FP32_ID) { e = set_smem_attr<PrecF>(); if (!e) e = occupancy<PrecF>(threads, p->smem, p->kt_t, p->threads_t, p->nc_t, p->smem_t, p->w_t, per_sm, per_sm_t); }
+	else { e = set_smem_attr<PrecX>(); if (!e) e = occupancy<PrecX>(threads, p->smem, p->kt_t, p->threads_t, p->nc_t, p->smem_t, p->w_t, per_sm, per_sm_t); }
 	if (e) { delete p; return nullptr; }
 	const long opt_cps = mgcu_option(MG_OPT_CTAS_PER_SM_ID);
 	if (opt_cps > 0) per_sm = (int)std::min<long>(per_sm, opt_cps);

@@ -113,6 +113,16 @@ int mg_target_set_resident(void* udata, int enable)
 	return 0;
 }
 
+int mg_target_conserves_weight(void* udata)
+{
+	mg_target_handle* h = (mg_target_handle*)udata;
+	if (!h || h->magic != MG_TARGET_MAGIC) { mg_set_error("mg_target_conserves_weight: invalid handle"); return -1; }
+	mgcu_lock();
+	const int n = mgcu_target_conserves_weight(h->dev);
+	mgcu_unlock();
+	return n;
+}
+
 int mg_target_sweep_gates(void* udata)
 {
 	mg_target_handle* h = (mg_target_handle*)udata;

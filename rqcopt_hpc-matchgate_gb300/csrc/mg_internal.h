@@ -34,7 +34,8 @@ extern "C" {
 #define MG_OPT_TARGET_THREADS_ID   6
 #define MG_OPT_TARGET_COLUMNS_ID   7
 #define MG_OPT_TRANSLATIONAL_INVARIANCE_ID 8
-#define MG_NOPTIONS             8
+#define MG_OPT_TARGET_DENSE_ID  9
+#define MG_NOPTIONS             9
 
 /* ---- runtime ---- */
 void mg_set_error(const char* fmt, ...);
@@ -69,6 +70,7 @@ int mgcu_target_apply(mgcu_target* t, const mgc* psi, mgc* out);      /* host ve
 int mgcu_target_L(const mgcu_target* t);
 void mgcu_target_set_resident(mgcu_target* t, int enable);
 int mgcu_target_sweep_gates(mgcu_target* t);
+int mgcu_target_conserves_weight(mgcu_target* t);
 
 /* ---- batched evaluation plans (the hot path) ---- */
 typedef struct

@@ -24,6 +24,7 @@ PREC_FP64, PREC_MIXED, PREC_FP32 = 0, 1, 2
 OPT_TILE_BITS, OPT_THREADS, OPT_CHUNK_COLUMNS, OPT_CTAS_PER_SM = 1, 2, 3, 4
 OPT_TARGET_TILE_BITS, OPT_TARGET_THREADS, OPT_TARGET_COLUMNS = 5, 6, 7
 OPT_TRANSLATIONAL_INVARIANCE = 8
+OPT_TARGET_DENSE = 9
 EVAL_TARGET, EVAL_GRADIENT, EVAL_HESSIAN, EVAL_TI = 0, 1, 2, 4
 
 P = C.c_void_p
@@ -119,6 +120,7 @@ class MatchgateLib:
             L.mg_target_free.argtypes = [P]
             L.mg_target_set_resident.argtypes = [P, C.c_int]
             L.mg_target_sweep_gates.argtypes = [P]
+            L.mg_target_conserves_weight.argtypes = [P]
             L.mg_batch_create.restype = P
             L.mg_batch_create.argtypes = [C.c_int, P, P, P, P, P, C.c_int]
             L.mg_batch_set_gates.argtypes = [P, C.c_int, P]

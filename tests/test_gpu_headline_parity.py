@@ -38,13 +38,20 @@ def _rel(x, y):
     return float(np.linalg.norm(x - y) / np.linalg.norm(y))
 
 
+@pytest.mark.parametrize("dense,target_threads", [(0, 0), (1, 0), (1, 128), (1, 256)])
 @pytest.mark.parametrize("prec,tol", [(mgcu.PREC_FP64, 1e-12), (mgcu.PREC_MIXED, 1e-9)])
-def test_headline_columns_vs_oracle(mglib, headline, prec, tol):
+def test_headline_columns_vs_oracle(mglib, headline, prec, tol, dense, target_threads):
+    """dense=0: the library's choice for this target, which conserves the Hamming weight
+    (the sweep touches only amplitudes of the column's weight); dense=1: every amplitude,
+    with target_threads threads per block (0: the library's choice; 128: eight quartets per
+    thread, 256: four)"""
     lib = mglib
     g, w, v, perms, ref = headline
     t = lib.target_circuit(g, w, L)
     assert lib.lib.mg_target_sweep_gates(mgcu.P(t)) == 1928   # fermionic swaps relabelled away
     lib.set_precision(prec)
+    lib.set_option(mgcu.OPT_TARGET_DENSE, dense)
+    lib.set_option(mgcu.OPT_TARGET_THREADS, target_threads)
     try:
         for r, (f_o, dv_o) in zip(RANGES, ref):
             rc, f, dv = lib.brickwall_columns(lib.mg_target_apply, t, v, perms, L, *r)
@@ -52,8 +59,32 @@ def test_headline_columns_vs_oracle(mglib, headline, prec, tol):
             assert abs(f - f_o) <= tol * abs(f_o), (r, f, f_o)
             assert _rel(dv, dv_o) <= tol, (r, _rel(dv, dv_o))
     finally:
+        lib.set_option(mgcu.OPT_TARGET_THREADS, 0)
+        lib.set_option(mgcu.OPT_TARGET_DENSE, 0)
         lib.set_precision(mgcu.PREC_FP64)
         lib.target_free(t)
+
+
+@pytest.mark.parametrize("prec", [mgcu.PREC_FP64, mgcu.PREC_MIXED, mgcu.PREC_FP32])
+def test_weight_restricted_sweep_is_bit_identical(mglib, prec):
+    """the weight-restricted sweep skips only quartets of zeros: f and the gradients equal
+    the full sweep's bit for bit (headline target, columns from both ends of the range)"""
+    lib = mglib
+    g, w, v, perms = bench.workload(L, NLAYERS, TROTTER_STEPS)
+    t = lib.target_circuit(g, w, L)
+    lib.set_precision(prec)
+    try:
+        out = []
+        for dense in (0, 1):
+            lib.set_option(mgcu.OPT_TARGET_DENSE, dense)
+            out.append([lib.brickwall_columns(lib.mg_target_apply, t, v, perms, L, *r) for r in [(0, 40), (65500, 65536)]])
+    finally:
+        lib.set_option(mgcu.OPT_TARGET_DENSE, 0)
+        lib.set_precision(mgcu.PREC_FP64)
+        lib.target_free(t)
+    for (rc0, f0, dv0), (rc1, f1, dv1) in zip(*out):
+        assert rc0 == 0 and rc1 == 0
+        assert f0 == f1 and np.array_equal(dv0, dv1)
 
 
 @pytest.mark.parametrize("prec,tol", [(mgcu.PREC_FP64, 1e-12), (mgcu.PREC_MIXED, 1e-9)])

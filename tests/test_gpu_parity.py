@@ -387,7 +387,8 @@ def test_algebra_on_gpu(lib, oracle):
 
 def _structured_gates(n, rng):
     """gates whose blocks are drawn from every structure the target sweep specialises:
-    identity, swap, diag(1,-1), diag(1,a), diagonal, anti-diagonal, real-or-imaginary, general"""
+    identity, swap, diag(1,-1), diag(1,a), diagonal, anti-diagonal, real-or-imaginary, general,
+    symmetric hop"""
     def block(kind):
         z = crandn((2, 2), rng)
         if kind == 0: return np.eye(2)
@@ -399,11 +400,14 @@ def _structured_gates(n, rng):
         if kind == 6:
             r = rng.standard_normal((2, 2))
             return np.where(rng.random((2, 2)) < 0.5, r + 0j, 1j * r)
+        if kind == 8:   # symmetric hop [[c, i s], [i s, c]] (its own kernel path)
+            th = rng.uniform(-np.pi, np.pi)
+            return np.array([[np.cos(th), 1j * np.sin(th)], [1j * np.sin(th), np.cos(th)]])
         return z
     out = np.zeros((n, 8), complex)
     for g in range(n):
-        out[g, :4] = block(rng.integers(8)).reshape(4)
-        out[g, 4:] = block(rng.integers(8)).reshape(4)
+        out[g, :4] = block(rng.integers(9)).reshape(4)
+        out[g, 4:] = block(rng.integers(9)).reshape(4)
     return out
 
 
@@ -455,7 +459,9 @@ def test_hubbard_target_vs_oracle(lib, oracle):
                                                       (14, 12, 128, mgcu.PREC_FP64), (14, 10, 0, mgcu.PREC_FP32),
                                                       (14, 0, 0, mgcu.PREC_FP32), (14, 13, 0, mgcu.PREC_MIXED),
                                                       (14, 13, 512, mgcu.PREC_MIXED), (14, 13, 512, mgcu.PREC_FP64),
-                                                      (14, 12, 512, mgcu.PREC_MIXED), (12, 0, 512, mgcu.PREC_FP64)])
+                                                      (14, 12, 512, mgcu.PREC_MIXED), (12, 0, 512, mgcu.PREC_FP64),
+                                                      (14, 12, 128, mgcu.PREC_MIXED), (14, 0, 128, mgcu.PREC_FP32),
+                                                      (16, 12, 128, mgcu.PREC_MIXED)])
 def test_target_sweep_tiles_vs_oracle(lib, oracle, L, tile_bits, threads, prec):
     """the target-sweep kernel with 1, 2, 4 and 8 quartets per thread, one or several
     tiles per pass and structured and general gates (also on the dropped qubit), against
