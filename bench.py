@@ -49,12 +49,12 @@ def parse():
     ap.add_argument("--no-fp64", action="store_true", help="leave the FP64 comparison out")
     ap.add_argument("--cpu-seconds", type=float, default=15.0, help="budget of the CPU baseline sample")
     ap.add_argument("--no-cpu", action="store_true")
-    ap.add_argument("--config", default="grad16", choices=["grad16", "grad18", "hess14", "batch64", "serve", "published"],
+    ap.add_argument("--config", default="grad16", choices=["grad16", "grad18", "hess14", "batch64", "serve", "published", "hostmap"],
                     help="grad16: the headline (L=16 gradient, 5 layers); grad18: L=18 gradient, 7 layers, on a "
                          "column sample; hess14: L=14 full Hessian, 9 layers; batch64: 64 instances of uneven size "
                          "in one batched launch sequence; serve: a seeded Poisson request stream through the "
                          "request server; published: one trust-region iteration of the reference's published "
-                         "benchmark (L=16, 5 layers, 601-layer target)")
+                         "benchmark (L=16, 5 layers, 601-layer target); hostmap: L=14 with the target as a host map")
     ap.add_argument("--published-hessian", default="both", choices=["plain", "ti", "both"])
     ap.add_argument("--published-precision", default="both", choices=["mixed", "fp64", "both"])
     ap.add_argument("--resident", action="store_true", help="--config published: keep the target columns on the GPU")
@@ -598,6 +598,70 @@ def run_published(a):
         "runs": rows, "accuracy": acc}))
 
 
+def run_hostmap(a):
+    """config hostmap: a target given as a caller's host map, the pattern of the reference's
+    drivers (benchmark_hpc/benchmark_threads.c:24-33 pass a host brickwall apply as `ufunc`):
+    L=14, 5-layer fit against a 16-layer random brickwall applied on the host (a plain C map
+    from tests/helpers), one projected-gradient evaluation with the map called from all host
+    threads and from one (the latter on a column sample, scaled), beside the same brickwall
+    as a GPU target and the oracle port on all host cores"""
+    import ctypes as C
+    import numpy as np
+    import mgcu
+    import targets as T
+    lib = mgcu.default_lib()
+    helpers = C.CDLL(os.path.join(ROOT, "tests", "_build", "libmgtest.so"))
+    L, nl, nu = 14, 5, 16
+    rng = np.random.default_rng(14)
+    ul, up = T.haar_matchgates(nu, rng), T.brickwall_perms(L, nu)
+    v, perms = T.near_identity_brickwall(nl, rng), T.brickwall_perms(L, nl)
+    g = np.ascontiguousarray(ul.reshape(-1, 8)); pp = np.ascontiguousarray(up.astype(np.int32))
+
+    class HB(C.Structure):
+        _fields_ = [("gates", C.c_void_p), ("perms", C.c_void_p), ("nlayers", C.c_int)]
+    hb = HB(g.ctypes.data, pp.ctypes.data, nu)
+    uf, ud = mgcu.ufunc_address(helpers.mgt_brickwall_ufunc), C.addressof(hb)
+    lib.set_precision(mgcu.PREC_FP64)
+    ncols = 1 << L
+    lib.brickwall_columns(uf, ud, v, perms, L, 0, 64)   # plans and module loading
+    t0 = time.perf_counter()
+    rc, f_all, g_all = lib.brickwall_projected_gradient(uf, ud, v, perms, L)
+    s_all = time.perf_counter() - t0
+    assert rc == 0, lib.last_error()
+    threads = os.cpu_count()
+    lib.set_option(mgcu.OPT_HOST_THREADS, 1)
+    sample = 512
+    t0 = time.perf_counter()
+    rc, _, _ = lib.brickwall_columns(uf, ud, v, perms, L, 0, sample)
+    s_one = (time.perf_counter() - t0) * ncols / sample
+    lib.set_option(mgcu.OPT_HOST_THREADS, 0)
+    t = lib.target_brickwall(ul, up, L)
+    lib.brickwall_projected_gradient(lib.mg_target_apply, t, v, perms, L)
+    t0 = time.perf_counter()
+    rc, f_gpu, g_gpu = lib.brickwall_projected_gradient(lib.mg_target_apply, t, v, perms, L)
+    s_gpu = time.perf_counter() - t0
+    lib.target_free(t)
+    out = {"metric": "projected-gradient evaluation with a host-map target, L=14 (seconds)", "value": s_all, "unit": "s",
+           "higher_is_better": False, "n_gpus": 1, "dtype": "f64",
+           "data": "synthetic (seed 14: 16-layer Haar brickwall target applied by a host C map; 5-layer near-identity fit)",
+           "config": {"workload": "matchgate_brickwall_unitary_target_and_projected_gradient with a host linear_func",
+                      "L": L, "nlayers": nl, "target_layers": nu},
+           "host_threads": threads, "host_map_all_threads_s": s_all,
+           "host_map_one_thread_s": s_one, "one_thread_sample": f"{sample} of {ncols} columns, scaled",
+           "gpu_target_s": s_gpu,
+           "rel_diff_host_map_vs_gpu_target": float(abs(f_all - f_gpu) / abs(f_gpu))}
+    if not a.no_cpu:
+        import oracle
+        tt = oracle.Target("brickwall", L, ulist=ul, uperms=up)
+        nc = threads * 32
+        t0 = time.perf_counter()
+        oracle.brickwall_projected_gradient(tt, v, perms, L, nthreads=threads, col_range=(0, nc))
+        cs = time.perf_counter() - t0
+        out["cpu_baseline"] = {"value": cs * ncols / nc, "unit": "s", "cores": threads, "kind": "port",
+                               "sample": f"{nc} of {ncols} columns in {cs:.1f} s, scaled to one evaluation"}
+    print(json.dumps(out))
+
+
 def batch_workload(n=64, seed=4):
     """64 instances: L ~ U{10,12,14,16}, fitted depth ~ U{3..9} (Haar-random layers),
     target = a random matchgate brickwall of twice the depth; seeded"""
@@ -768,6 +832,8 @@ def main():
         run_serve(a)
     elif a.config == "published":
         run_published(a)
+    elif a.config == "hostmap":
+        run_hostmap(a)
     elif a.config != "grad16":
         run_secondary(a)
     else:

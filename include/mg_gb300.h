@@ -40,10 +40,14 @@ int mg_get_precision(void);
  * 715, 819); 0 (default) is the reference's plain build.
  * TARGET_DENSE: 1 sweeps every amplitude of a GPU circuit target even when all its gates
  * conserve the Hamming weight (by default such targets are swept on the amplitudes of the
- * basis column's weight only; both give bit-identical results). */
+ * basis column's weight only; both give bit-identical results).
+ * HOST_THREADS: host threads that call a caller's linear_func (a host map, not a GPU target)
+ * concurrently, one basis column per call, as the reference's OpenMP threads do; the map must
+ * be re-entrant (it is for the reference's own maps).  0 = the online cores; results do not
+ * depend on the count. */
 enum { MG_OPT_TILE_BITS = 1, MG_OPT_THREADS = 2, MG_OPT_CHUNK_COLUMNS = 3, MG_OPT_CTAS_PER_SM = 4,
        MG_OPT_TARGET_TILE_BITS = 5, MG_OPT_TARGET_THREADS = 6, MG_OPT_TARGET_COLUMNS = 7,
-       MG_OPT_TRANSLATIONAL_INVARIANCE = 8, MG_OPT_TARGET_DENSE = 9 };
+       MG_OPT_TRANSLATIONAL_INVARIANCE = 8, MG_OPT_TARGET_DENSE = 9, MG_OPT_HOST_THREADS = 10 };
 int mg_set_option(int option, long value);
 long mg_get_option(int option);
 

@@ -7,8 +7,10 @@
  */
 #include <stdint.h>
 #include <stdio.h>
+#include <pthread.h>
 #include <stdlib.h>
 #include <string.h>
+#include <unistd.h>
 
 #include "matchgate_target.h"
 #include "mg_gb300.h"
@@ -261,32 +263,53 @@ static mgcu_plan* get_plan(int L, int ngates, const int* wires, int nblocks, con
  * evaluation driver
  * ====================================================================================== */
 
-/* -conj(U e_b) on b's parity sector for b in [c0, c1), from a host linear_func */
-static int materialise(linear_func ufunc, void* udata, int L, long c0, long c1, mgc* cols)
+/* -conj(U e_b) on b's parity sector for b in [c0, c1), from a host linear_func.  The caller's
+ * map is called from several host threads at once, as the reference calls it from its
+ * OpenMP threads (src/matchgate_target.c:788-795); each thread owns its input and output
+ * vectors and the columns b = c0 + tid (mod nthreads), so the result does not depend on
+ * the thread count. */
+typedef struct
 {
-	const long n = 1L << L, S = n >> 1;
+	linear_func ufunc;
+	void* udata;
+	int L, nthreads, tid;
+	long c0, c1;
+	mgc* cols;
+	int* failed;     /* shared: set by the first failing call, stops the others */
+	int rc;          /* this thread's result */
+} mat_job;
+
+static void* mat_worker(void* arg)
+{
+	mat_job* j = (mat_job*)arg;
+	const long n = 1L << j->L, S = n >> 1;
 	struct statevector psi, out;
-	if (allocate_statevector(L, &psi) < 0 || allocate_statevector(L, &out) < 0)
+	j->rc = 0;
+	if (allocate_statevector(j->L, &psi) < 0) { j->rc = MG_ERR_ALLOC; __atomic_store_n(j->failed, 1, __ATOMIC_RELAXED); return NULL; }
+	if (allocate_statevector(j->L, &out) < 0)
 	{
 		free_statevector(&psi);
-		return MG_ERR_ALLOC;
+		j->rc = MG_ERR_ALLOC;
+		__atomic_store_n(j->failed, 1, __ATOMIC_RELAXED);
+		return NULL;
 	}
 	memset(psi.data, 0, sizeof(numeric) * n);
-	int rc = 0;
-	for (long b = c0; b < c1 && !rc; b++)
+	for (long b = j->c0 + j->tid; b < j->c1; b += j->nthreads)
 	{
+		if (__atomic_load_n(j->failed, __ATOMIC_RELAXED)) break;
 		psi.data[b] = 1;
-		const int ret = ufunc(&psi, udata, &out);
+		const int ret = j->ufunc(&psi, j->udata, &out);
 		psi.data[b] = 0;
 		if (ret < 0)
 		{
 			fprintf(stderr, "call of 'ufunc' failed, return value: %i\n", ret);
 			mg_set_error("call of 'ufunc' failed, return value: %i", ret);
-			rc = MG_ERR_UFUNC;
+			j->rc = MG_ERR_UFUNC;
+			__atomic_store_n(j->failed, 1, __ATOMIC_RELAXED);
 			break;
 		}
 		const int pb = __builtin_popcountl(b) & 1;
-		mgc* col = cols + (size_t)(b - c0) * S;
+		mgc* col = j->cols + (size_t)(b - j->c0) * S;
 		for (long c = 0; c < S; c++)
 		{
 			const long a = (c << 1) | ((__builtin_popcountl(c) + pb) & 1);
@@ -295,6 +318,42 @@ static int materialise(linear_func ufunc, void* udata, int L, long c0, long c1, 
 	}
 	free_statevector(&out);
 	free_statevector(&psi);
+	return NULL;
+}
+
+/* host threads for a host map: MG_OPT_HOST_THREADS, else the online cores */
+static int host_threads(long ncols)
+{
+	long t = mgcu_option(MG_OPT_HOST_THREADS_ID);
+	if (t <= 0) t = sysconf(_SC_NPROCESSORS_ONLN);
+	if (t < 1) t = 1;
+	if (t > 256) t = 256;
+	if (t > ncols) t = ncols;
+	return (int)t;
+}
+
+static int materialise(linear_func ufunc, void* udata, int L, long c0, long c1, mgc* cols)
+{
+	if (c1 <= c0) return 0;
+	const int nt = host_threads(c1 - c0);
+	int failed = 0;
+	mat_job* jobs = calloc((size_t)nt, sizeof(mat_job));
+	pthread_t* th = calloc((size_t)nt, sizeof(pthread_t));
+	if (!jobs || !th) { free(jobs); free(th); return MG_ERR_ALLOC; }
+	int started = 0;
+	for (int t = 0; t < nt; t++)
+	{
+		jobs[t] = (mat_job){ ufunc, udata, L, nt, t, c0, c1, cols, &failed, 0 };
+		if (t == 0) continue;   /* the calling thread takes share 0 */
+		if (pthread_create(&th[t], NULL, mat_worker, &jobs[t]) != 0) { jobs[t].rc = MG_ERR_ALLOC; failed = 1; break; }
+		started = t;
+	}
+	if (!failed) mat_worker(&jobs[0]);
+	for (int t = 1; t <= started; t++) pthread_join(th[t], NULL);
+	int rc = 0;
+	for (int t = 0; t < nt && !rc; t++) rc = jobs[t].rc;
+	free(jobs);
+	free(th);
 	return rc;
 }
 
@@ -342,7 +401,12 @@ static int run_eval(linear_func ufunc, void* udata, const eval_req* q)
 		if (th) rc = mgcu_plan_columns(p, b0, b1, NULL);
 		else
 		{
-			const long chunk = mgcu_plan_chunk_columns(p);
+			/* chunks of at most 1/8 of the range (at least 1024 columns): the caller's map fills
+			 * chunk k + 1 on the host threads while the GPU works on chunk k (the copy of a
+			 * chunk from this pageable buffer completes before its call returns) */
+			long chunk = mgcu_plan_chunk_columns(p);
+			const long part = (b1 - b0 + 7) / 8 > 1024 ? (b1 - b0 + 7) / 8 : 1024;
+			if (chunk > part) chunk = part;
 			const long S = ncols >> 1;
 			mgc* cols = malloc(sizeof(mgc) * S * (size_t)(chunk < b1 - b0 ? chunk : b1 - b0 > 0 ? b1 - b0 : 1));
 			if (!cols) rc = MG_ERR_ALLOC;

@@ -35,7 +35,8 @@ extern "C" {
 #define MG_OPT_TARGET_COLUMNS_ID   7
 #define MG_OPT_TRANSLATIONAL_INVARIANCE_ID 8
 #define MG_OPT_TARGET_DENSE_ID  9
-#define MG_NOPTIONS             9
+#define MG_OPT_HOST_THREADS_ID  10
+#define MG_NOPTIONS             10
 
 /* ---- runtime ---- */
 void mg_set_error(const char* fmt, ...);

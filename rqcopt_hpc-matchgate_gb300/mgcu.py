@@ -25,6 +25,7 @@ OPT_TILE_BITS, OPT_THREADS, OPT_CHUNK_COLUMNS, OPT_CTAS_PER_SM = 1, 2, 3, 4
 OPT_TARGET_TILE_BITS, OPT_TARGET_THREADS, OPT_TARGET_COLUMNS = 5, 6, 7
 OPT_TRANSLATIONAL_INVARIANCE = 8
 OPT_TARGET_DENSE = 9
+OPT_HOST_THREADS = 10
 EVAL_TARGET, EVAL_GRADIENT, EVAL_HESSIAN, EVAL_TI = 0, 1, 2, 4
 
 P = C.c_void_p
