@@ -44,10 +44,18 @@ int mg_get_precision(void);
  * HOST_THREADS: host threads that call a caller's linear_func (a host map, not a GPU target)
  * concurrently, one basis column per call, as the reference's OpenMP threads do; the map must
  * be re-entrant (it is for the reference's own maps).  0 = the online cores; results do not
- * depend on the count. */
+ * depend on the count.
+ * FIT_CACHE: how a gradient evaluation gets each fitted gate's input in the backward sweep.
+ * 0 or 1 (default): the reference's cache of every gate's input state
+ * (src/matchgate_brickwall.c:52-127); 2: only each pass's output state is kept and the inputs
+ * are recovered with the gates' block inverses (one state per pass and block instead of one
+ * per gate, much less device memory and traffic, but a third more arithmetic and about 25 %
+ * slower in float-float at L=16-18; gates that are not invertible fall back to the cache).
+ * Hessian evaluations always cache. */
 enum { MG_OPT_TILE_BITS = 1, MG_OPT_THREADS = 2, MG_OPT_CHUNK_COLUMNS = 3, MG_OPT_CTAS_PER_SM = 4,
        MG_OPT_TARGET_TILE_BITS = 5, MG_OPT_TARGET_THREADS = 6, MG_OPT_TARGET_COLUMNS = 7,
-       MG_OPT_TRANSLATIONAL_INVARIANCE = 8, MG_OPT_TARGET_DENSE = 9, MG_OPT_HOST_THREADS = 10 };
+       MG_OPT_TRANSLATIONAL_INVARIANCE = 8, MG_OPT_TARGET_DENSE = 9, MG_OPT_HOST_THREADS = 10,
+       MG_OPT_FIT_CACHE = 11 };
 int mg_set_option(int option, long value);
 long mg_get_option(int option);
 
@@ -95,6 +103,13 @@ int mg_target_conserves_weight(void* udata);
 int mg_optimize_brickwall(void* target, const struct matchgate vlist0[], int nlayers, int nqubits, const int* perms[],
                           const struct rtr_params* params, int niter, double refine_gnorm, double f_iter[], int prec_iter[],
                           struct matchgate vlist_out[]);
+/* The same fit with one parameter block per gate of a general circuit (gates0 on wires
+ * [2 ngates], 8 ngates real parameters; the per-gate Riemannian gradient and Hessian of
+ * matchgate_circuit_unitary_target_gradient_vector_hessian_matrix), retraction per gate.
+ * The reference optimises per layer only; this is the per-gate extension of that loop. */
+int mg_optimize_circuit(void* target, const struct matchgate gates0[], int ngates, const int wires[], int nqubits,
+                        const struct rtr_params* params, int niter, double refine_gnorm, double f_iter[], int prec_iter[],
+                        struct matchgate gates_out[]);
 
 /* ---------------------------------------------------------------------------------
  * Target construction (the reference builds its benchmark targets in Python,
@@ -193,6 +208,20 @@ int matchgate_circuit_unitary_target_gradient_hessian(linear_func ufunc, void* u
 	const struct matchgate gates[], const int ngates, const int wires[], const int nqubits,
 	numeric* fval, struct matchgate dgates[], numeric* hess);
 
+/* Per-gate Riemannian forms of a general circuit: grad_vec [8 ngates] and H [(8 ngates)^2]
+ * (row-major, H[(g*8+x)*m + h*8+y]), the projection of the reference's per-layer
+ * matchgate_brickwall_unitary_target_gradient_vector_hessian_matrix (src/matchgate_target.c:
+ * 877-973) applied with one block per gate: gradient conjugated and mapped by
+ * tangent_matchgate_to_real, Hessian blocks contracted with real_to_tangent unit vectors,
+ * conjugated, projected, with the -1/2 (Z dV^dagger V + V dV^dagger Z) term on diagonal
+ * blocks.  Summing the blocks of the gates of each layer gives the per-layer forms. */
+int matchgate_circuit_unitary_target_and_projected_gradient(linear_func ufunc, void* udata,
+	const struct matchgate gates[], const int ngates, const int wires[], const int nqubits,
+	numeric* fval, double* grad_vec);
+int matchgate_circuit_unitary_target_gradient_vector_hessian_matrix(linear_func ufunc, void* udata,
+	const struct matchgate gates[], const int ngates, const int wires[], const int nqubits,
+	numeric* fval, double* grad_vec, double* H);
+
 /* Partial traces over the basis columns b in [col_begin, col_end): the column range
  * the reference gives each MPI rank (benchmark_hpc/benchmark_mpi.c:26-45).  Summing
  * the results of disjoint ranges gives the full trace. */
@@ -210,6 +239,10 @@ enum { MG_EVAL_TARGET = 0, MG_EVAL_GRADIENT = 1, MG_EVAL_HESSIAN = 2, MG_EVAL_TI
 typedef struct mg_plan mg_plan;
 mg_plan* mg_plan_brickwall(linear_func ufunc, void* udata, const struct matchgate vlist[], int nlayers, int nqubits,
 	const int* perms[], int what);
+/* a plan of a general circuit with one parameter block per gate (what: TARGET, GRADIENT or
+ * HESSIAN; mg_plan_set_gates takes the ngates gates, the results are per gate) */
+mg_plan* mg_plan_circuit(linear_func ufunc, void* udata, const struct matchgate gates[], int ngates, const int wires[],
+	int nqubits, int what);
 int mg_plan_set_gates(mg_plan* plan, const struct matchgate vlist[]);
 int mg_plan_run(mg_plan* plan);
 /* any output pointer may be NULL; grad_vec/H are the projected (Riemannian) forms */

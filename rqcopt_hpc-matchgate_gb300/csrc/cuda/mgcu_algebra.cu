@@ -160,9 +160,9 @@ __global__ void k_dense_matvec(const double2* __restrict__ U, long n, const doub
 
 #define TRY(x) do { int _r = (x); if (_r) return _r; } while (0)
 
-int up(DevBuf& b, const void* h, size_t n) { TRY(b.alloc(n)); MGCU_TRY(cudaMemcpyAsync(b.p, h, n, cudaMemcpyHostToDevice, mgcu_ctx()->stream)); return 0; }
-int down(void* h, const DevBuf& b, size_t n) { MGCU_TRY(cudaMemcpyAsync(h, b.p, n, cudaMemcpyDeviceToHost, mgcu_ctx()->stream)); return 0; }
-int sync() { MGCU_TRY(cudaStreamSynchronize(mgcu_ctx()->stream)); return 0; }
+int up(DevBuf& b, const void* h, size_t n) { TRY(b.alloc(n)); MGCU_TRY(cudaMemcpyAsync(b.p, h, n, cudaMemcpyHostToDevice, mgcu_stream())); return 0; }
+int down(void* h, const DevBuf& b, size_t n) { MGCU_TRY(cudaMemcpyAsync(h, b.p, n, cudaMemcpyDeviceToHost, mgcu_stream())); return 0; }
+int sync() { MGCU_TRY(cudaStreamSynchronize(mgcu_stream())); return 0; }
 
 }  // namespace
 
@@ -174,15 +174,15 @@ int mgcu_project_dev(const mgg* vblocks, int nb, const double* dgrad_dev, const 
 	TRY(up(g_v, vblocks, sizeof(mgg) * nb));
 	TRY(g_dv.alloc(sizeof(mgg) * nb));
 	TRY(g_gv.alloc(sizeof(double) * m));
-	k_project_grad<<<(nb + 63) / 64, 64, 0, c->stream>>>(g_v.as<mgg>(), dgrad_dev, nb, g_gv.as<double>(), g_dv.as<mgg>());
+	k_project_grad<<<(nb + 63) / 64, 64, 0, mgcu_stream()>>>(g_v.as<mgg>(), dgrad_dev, nb, g_gv.as<double>(), g_dv.as<mgg>());
 	MGCU_LAUNCHED();
 	if (grad_vec) TRY(down(grad_vec, g_gv, sizeof(double) * m));
 	if (hess_dev && H)
 	{
 		TRY(g_H.alloc(sizeof(double) * m * m));
-		k_project_hess<<<(nb * nb * 8 + 63) / 64, 64, 0, c->stream>>>(g_v.as<mgg>(), g_dv.as<mgg>(), (const double2*)hess_dev, nb, g_H.as<double>());
+		k_project_hess<<<(nb * nb * 8 + 63) / 64, 64, 0, mgcu_stream()>>>(g_v.as<mgg>(), g_dv.as<mgg>(), (const double2*)hess_dev, nb, g_H.as<double>());
 		MGCU_LAUNCHED();
-		k_mirror_real<<<(m * m + 255) / 256, 256, 0, c->stream>>>(m, g_H.as<double>());
+		k_mirror_real<<<(m * m + 255) / 256, 256, 0, mgcu_stream()>>>(m, g_H.as<double>());
 		MGCU_LAUNCHED();
 		TRY(down(H, g_H, sizeof(double) * m * m));
 	}
@@ -196,7 +196,7 @@ extern "C" int mgcu_retract(const mgg* u, const double* eta, int n, mgg* v)
 	TRY(up(g_u, u, sizeof(mgg) * n));
 	TRY(up(g_eta, eta, sizeof(double) * 8 * n));
 	TRY(g_v.alloc(sizeof(mgg) * n));
-	k_retract<<<(n + 63) / 64, 64, 0, c->stream>>>(g_u.as<mgg>(), g_eta.as<double>(), n, g_v.as<mgg>());
+	k_retract<<<(n + 63) / 64, 64, 0, mgcu_stream()>>>(g_u.as<mgg>(), g_eta.as<double>(), n, g_v.as<mgg>());
 	MGCU_LAUNCHED();
 	TRY(down(v, g_v, sizeof(mgg) * n));
 	return sync();
@@ -211,7 +211,7 @@ extern "C" int mgcu_truncated_cg(const double* grad, const double* hess, int n, 
 	TRY(g_z.alloc(sizeof(double) * n));
 	TRY(g_x.alloc(sizeof(double) * 3 * n));
 	TRY(g_flag.alloc(sizeof(int)));
-	k_tcg<<<1, 512, 0, c->stream>>>(g_grad.as<double>(), g_hess.as<double>(), n, radius, maxiter, abstol, reltol, g_z.as<double>(), g_x.as<double>(), g_flag.as<int>());
+	k_tcg<<<1, 512, 0, mgcu_stream()>>>(g_grad.as<double>(), g_hess.as<double>(), n, radius, maxiter, abstol, reltol, g_z.as<double>(), g_x.as<double>(), g_flag.as<int>());
 	MGCU_LAUNCHED();
 	int flag = 0;
 	TRY(down(z, g_z, sizeof(double) * n));
@@ -227,7 +227,7 @@ extern "C" int mgcu_matvec(const double* H, const double* x, int n, double* y)
 	TRY(up(g_hess, H, sizeof(double) * n * n));
 	TRY(up(g_x, x, sizeof(double) * n));
 	TRY(g_y.alloc(sizeof(double) * n));
-	k_matvec<<<(n + 127) / 128, 128, 0, c->stream>>>(g_hess.as<double>(), g_x.as<double>(), n, g_y.as<double>());
+	k_matvec<<<(n + 127) / 128, 128, 0, mgcu_stream()>>>(g_hess.as<double>(), g_x.as<double>(), n, g_y.as<double>());
 	MGCU_LAUNCHED();
 	TRY(down(y, g_y, sizeof(double) * n));
 	return sync();
@@ -240,7 +240,7 @@ extern "C" int mgcu_dense_matvec(const void* U, int L, const mgc* psi, mgc* out)
 	const long n = 1L << L;
 	TRY(up(g_x, psi, sizeof(double2) * n));
 	TRY(g_y.alloc(sizeof(double2) * n));
-	k_dense_matvec<<<(int)((n + 127) / 128), 128, 0, c->stream>>>((const double2*)U, n, g_x.as<double2>(), g_y.as<double2>());
+	k_dense_matvec<<<(int)((n + 127) / 128), 128, 0, mgcu_stream()>>>((const double2*)U, n, g_x.as<double2>(), g_y.as<double2>());
 	MGCU_LAUNCHED();
 	TRY(down(out, g_y, sizeof(double2) * n));
 	return sync();

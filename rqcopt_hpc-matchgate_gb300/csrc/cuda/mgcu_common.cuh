@@ -21,6 +21,7 @@ struct MgcuContext
 };
 
 MgcuContext* mgcu_ctx();                 // initialises on first use; NULL on failure
+cudaStream_t mgcu_stream();              // the calling host thread's stream (default: the library's)
 void mgcu_count_launch(long n = 1);
 int mgcu_check(cudaError_t e, const char* what, const char* file, int line);
 

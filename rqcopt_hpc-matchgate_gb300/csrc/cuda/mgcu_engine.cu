@@ -21,6 +21,7 @@
 #include "mgcu_common.cuh"
 
 #include <algorithm>
+#include <cmath>
 #include <array>
 #include <map>
 #include <memory>
@@ -253,6 +254,8 @@ struct Args
 	long S;                    // 2^(L-1)
 	ProgDev W, U;
 	const T* wm;               // W gate matrices [ngates][8]: c0..c3, k0..k3
+	const T* wmi;              // their block inverses (k_columns_adj)
+	T* ck;                     // k_columns_adj: per block, each pass's output state [npass][S]
 	const T* um;               // target gate matrices
 	const int* ukind;          // target block kinds (null: every block general)
 	const TGate* utg;          // target gate records (k_target)
@@ -888,7 +891,10 @@ __device__ __forceinline__ void tgt_gate_any(unsigned tb, unsigned td, const TGa
 		const unsigned sgk[1] = { ((unsigned)__popc(e & ml) + sn + (md ? pe : 0u)) & 1u };
 		const unsigned sgc[1] = { sgk[0] ^ md };
 		tgt_block<P, 1, true, NC>(tb, td, x, 0u, MW, (kw >> 3) & 7, (kw >> 10) & 15, m + 4 * ES, sgk);
-		tgt_block<P, 1, true, NC>(tb, td, x, MY, MZ, kw & 7, (kw >> 6) & 15, m, sgc);
+		// the same arithmetic as the other sweep paths (hops by tgt_hop), so that every tile
+		// and block size gives bit-identical columns
+		if (kw_hop_center(kw)) tgt_hop<P, 1, true, NC>(tb, td, x, MY, MZ, m, sgc);
+		else tgt_block<P, 1, true, NC>(tb, td, x, MY, MZ, kw & 7, (kw >> 6) & 15, m, sgc);
 	}
 }
 
@@ -1392,6 +1398,123 @@ __global__ void __launch_bounds__(256, 2) k_columns(Args<P> a)
 	block_reduce1<P>(facc, s.red, a.part_f + (size_t)blockIdx.x * 2);
 }
 
+// f and gate gradients of one column without cached gate inputs (gradient plans with
+// invertible fitted gates): the forward sweep keeps each pass's output state (a checkpoint;
+// the state is written at the end of every pass anyway, to hand it to the next pass), and the
+// backward sweep reloads the output of the pass it is in and recovers each gate's input by
+// applying the gate's block inverses (computed on the host), in the same quartet loop as the
+// transposed derivative and the gradient contraction, so no barrier separates them.  Two
+// tiles per block (the state and the derivative).  Reference: the backward sweep of
+// src/matchgate_brickwall.c:87-127, whose inputs come from the forward cache there.
+template <class P>
+__device__ __forceinline__ void w_column_adj(const Args<P>& a, long b, long prow, typename P::T* su, typename P::T* ck,
+	typename P::Acc& facc, char* smem_raw)
+{
+	typedef typename P::T T;
+	const int kt = a.kt, Q = 1 << (kt - 2);
+	T* ft = reinterpret_cast<T*>(smem_raw);   // the state
+	T* tile;                                  // the forward sweep's state, then the derivative
+	Smem s = smem_layout<T>(smem_raw + sizeof(T) * ((size_t)1 << kt), kt, tile);
+	const long S = a.S;
+	const int par = __popcll(b) & 1;
+	const unsigned cb = (unsigned)(b >> 1);
+	const T* dsrc = a.dense + (size_t)(b - a.dense_b0) * S;
+	const int np = a.W.npass;
+	for (int p = 0; p < np; p++)
+	{
+		const PassRec& pr = a.W.pass[p];
+		__syncthreads();
+		setup_pass(pr, kt, s);
+		__syncthreads();
+		const unsigned ntile = 1u << pr.nnl;
+		const bool last = p == np - 1;
+		for (unsigned tau = 0; tau < ntile; tau++)
+		{
+			const unsigned nlb = nl_base(pr, tau);
+			const int tpar = (__popcll(nlb) + par) & 1;
+			if (p == 0) tile_load_basis<P>(tile, kt, s, nlb, cb);
+			else tile_load<P>(tile, kt, s, nlb, ck + (size_t)(p - 1) * S);
+			__syncthreads();
+			for (int gi = pr.gbeg; gi < pr.gend; gi++)
+			{
+				const GateRec r = a.W.gate[gi];
+				gate_forward<P>(tile, r, load_gate(a.wm, r.g), Q, tpar, nullptr, s, nlb);
+				__syncthreads();
+			}
+			if (last)
+				for (unsigned e = threadIdx.x; e < (1u << kt); e += blockDim.x)
+					P::acc_mul_add(facc, dsrc[gidx(s, nlb, e)], tile[e]);
+			tile_store<P>(tile, kt, s, nlb, ck + (size_t)p * S, false);
+			__syncthreads();
+		}
+	}
+	int nred = 0;
+	for (int p = np - 1; p >= 0; p--)
+	{
+		const PassRec& pr = a.W.pass[p];
+		__syncthreads();
+		setup_pass(pr, kt, s);
+		__syncthreads();
+		const unsigned ntile = 1u << pr.nnl;
+		for (unsigned tau = 0; tau < ntile; tau++)
+		{
+			const unsigned nlb = nl_base(pr, tau);
+			const int tpar = (__popcll(nlb) + par) & 1;
+			tile_load<P>(tile, kt, s, nlb, (p == np - 1) ? dsrc : su);
+			tile_load<P>(ft, kt, s, nlb, ck + (size_t)p * S);
+			__syncthreads();
+			for (int gi = pr.gend - 1; gi >= pr.gbeg; gi--)
+			{
+				const GateRec r = a.W.gate[gi];
+				const Gate8<T> G = load_gate(a.wm, r.g), Gi = load_gate(a.wmi, r.g);
+				typename P::Acc acc[8];
+#pragma unroll
+				for (int e = 0; e < 8; e++) acc[e] = P::acc_zero();
+				for (unsigned q = threadIdx.x; q < (unsigned)Q; q += blockDim.x)
+				{
+					unsigned ex, ew, ey, ez;
+					quartet(r, q, tpar, ex, ew, ey, ez);
+					const T fx = ft[ex], fw = ft[ew], fy = ft[ey], fz = ft[ez];
+					// the gate's input: its inverse applied to its output
+					const T x = P::madd2(Gi.k0, fx, Gi.k1, fw), w = P::madd2(Gi.k2, fx, Gi.k3, fw);
+					const T y = P::madd2(Gi.c0, fy, Gi.c1, fz), z = P::madd2(Gi.c2, fy, Gi.c3, fz);
+					ft[ex] = x; ft[ew] = w; ft[ey] = y; ft[ez] = z;
+					const T dx = tile[ex], dw = tile[ew], dy = tile[ey], dz = tile[ez];
+					contract_quartet<P>(acc, dx, dw, dy, dz, x, w, y, z);
+					// transpose (no conjugation): reference src/gate.c:725-728
+					tile[ex] = P::madd2(G.k0, dx, G.k2, dw);
+					tile[ew] = P::madd2(G.k1, dx, G.k3, dw);
+					tile[ey] = P::madd2(G.c0, dy, G.c2, dz);
+					tile[ez] = P::madd2(G.c1, dy, G.c3, dz);
+				}
+				block_reduce8<P>(acc, s.red, a.part_g + ((size_t)prow * a.ngates + r.g) * 16, 1.0, nred);
+			}
+			if (p > 0) tile_store<P>(tile, kt, s, nlb, su, false);
+			__syncthreads();
+		}
+	}
+}
+
+// 128 threads, three blocks per SM: the state, the derivative, both gates' blocks and the
+// eight accumulators fit in 168 registers without spilling
+constexpr int ADJ_THREADS = 128;
+
+template <class P>
+__global__ void __launch_bounds__(ADJ_THREADS, 3) k_columns_adj(Args<P> a)
+{
+	typedef typename P::T T;
+	extern __shared__ __align__(16) char smem_raw[];
+	const long S = a.S;
+	typename P::Acc facc = P::acc_zero();
+	T* su = a.su + (size_t)blockIdx.x * S;
+	T* ck = a.ck + (size_t)blockIdx.x * a.W.npass * S;
+	for (long b = a.b0 + blockIdx.x; b < a.b1; b += gridDim.x)
+		w_column_adj<P>(a, b, blockIdx.x, su, ck, facc, smem_raw);
+	T* tile;
+	Smem s = smem_layout<T>(smem_raw + sizeof(T) * ((size_t)1 << a.kt), a.kt, tile);
+	block_reduce1<P>(facc, s.red, a.part_f + (size_t)blockIdx.x * 2);
+}
+
 // batched items of one tile class (quartets per thread in the target sweep: QPT), target
 // and fitted circuit per column: the target column goes into the
 // block's slot sx, then the fitted circuit runs against it; slots and gate cache live in
@@ -1716,7 +1839,7 @@ static int upload_target_mats(const mgg* gates, int ng, DevBuf& buf, DevBuf& kin
 	int e = buf.alloc(sizeof(T) * h.size());
 	if (!e) e = kinds.alloc(sizeof(int) * k.size());
 	if (e) return e;
-	cudaStream_t st = mgcu_ctx()->stream;
+	cudaStream_t st = mgcu_stream();
 	MGCU_TRY(cudaMemcpyAsync(buf.p, h.data(), sizeof(T) * h.size(), cudaMemcpyHostToDevice, st));
 	MGCU_TRY(cudaMemcpyAsync(kinds.p, k.data(), sizeof(int) * k.size(), cudaMemcpyHostToDevice, st));
 	MGCU_TRY(cudaStreamSynchronize(st));
@@ -1835,14 +1958,46 @@ static int upload_mats(const mgg* gates, int ng, DevBuf& buf)
 		}
 	int e = buf.alloc(sizeof(T) * h.size());
 	if (e) return e;
-	MGCU_TRY(cudaMemcpyAsync(buf.p, h.data(), sizeof(T) * h.size(), cudaMemcpyHostToDevice, mgcu_ctx()->stream));
-	MGCU_TRY(cudaStreamSynchronize(mgcu_ctx()->stream));
+	MGCU_TRY(cudaMemcpyAsync(buf.p, h.data(), sizeof(T) * h.size(), cudaMemcpyHostToDevice, mgcu_stream()));
+	MGCU_TRY(cudaStreamSynchronize(mgcu_stream()));
+	return 0;
+}
+
+// the 2x2 block inverses of the gates (k_columns_adj); 1 when every block is invertible with
+// |det| at least 1e-8 of its largest entry squared, 0 otherwise (nothing uploaded then)
+template <class P>
+static int upload_inverses(const mgg* gates, int ng, DevBuf& buf, bool& ok)
+{
+	typedef typename P::T T;
+	std::vector<T> h((size_t)std::max(ng, 1) * 8);
+	ok = true;
+	auto inv = [&](const mgc* e, T* out) {
+		const mgc det = mgc_sub(mgc_mul(e[0], e[3]), mgc_mul(e[1], e[2]));
+		double mx = 0;
+		for (int q = 0; q < 4; q++) mx = std::max(mx, std::hypot(e[q].re, e[q].im));
+		const double d2 = det.re * det.re + det.im * det.im;
+		if (!(std::sqrt(d2) >= 1e-8 * mx * mx) || mx == 0) { ok = false; return; }
+		const mgc id = mgc_make(det.re / d2, -det.im / d2);   // 1 / det
+		const mgc r[4] = { mgc_mul(e[3], id), mgc_mul(mgc_make(-e[1].re, -e[1].im), id),
+			mgc_mul(mgc_make(-e[2].re, -e[2].im), id), mgc_mul(e[0], id) };
+		for (int q = 0; q < 4; q++) out[q] = P::make(r[q].re, r[q].im);
+	};
+	for (int g = 0; g < ng && ok; g++)
+	{
+		inv(gates[g].c, &h[(size_t)g * 8]);
+		inv(gates[g].k, &h[(size_t)g * 8 + 4]);
+	}
+	if (!ok) return 0;
+	int e = buf.alloc(sizeof(T) * h.size());
+	if (e) return e;
+	MGCU_TRY(cudaMemcpyAsync(buf.p, h.data(), sizeof(T) * h.size(), cudaMemcpyHostToDevice, mgcu_stream()));
+	MGCU_TRY(cudaStreamSynchronize(mgcu_stream()));
 	return 0;
 }
 
 static int upload_sched(const Sched& s, DevBuf& pass, DevBuf& gate)
 {
-	cudaStream_t st = mgcu_ctx()->stream;
+	cudaStream_t st = mgcu_stream();
 	int e = pass.alloc(sizeof(PassRec) * std::max<size_t>(s.pass.size(), 1));
 	if (e) return e;
 	e = gate.alloc(sizeof(GateRec) * std::max<size_t>(s.gate.size(), 1));
@@ -2152,6 +2307,9 @@ struct mgcu_plan
 	long chunk;
 	Sched ws;
 	DevBuf d_pass, d_gate, d_mats, d_pass_of, d_block, d_place, d_placew;
+	bool adj = false;              // gradient plan: checkpointed backward sweep (k_columns_adj)
+	bool adj_ok = false;           // the current gates are invertible (else the cached sweep)
+	DevBuf d_mats_inv, ck;
 	DevBuf su, sw, sh, cache, dcache, part_f, part_g, part_h, cols64, cols;
 	DevBuf out_f, out_g, out_blk, out_h, flush;
 	int nparts_h;
@@ -2191,12 +2349,12 @@ static int launch_target(mgcu_plan* p, long b0, long b1, typename P::T* out)
 			MGCU_TRY(cudaEventCreate(&ev));
 			p->kev.push_back(ev);
 		}
-	if (p->ktime) MGCU_TRY(cudaEventRecord(p->kev[p->kev_used], c->stream));
+	if (p->ktime) MGCU_TRY(cudaEventRecord(p->kev[p->kev_used], mgcu_stream()));
 	void (*kern)(Args<P>) = p->w_t ? k_target_w<P> : target_kernel<P>(p->kt_t, p->threads_t, p->nc_t);
 	if (!kern) { mg_set_error("no target-sweep kernel for 2^%d amplitudes and %d threads", p->kt_t, p->threads_t); return MG_ERR_ARG; }
-	kern<<<grid, p->threads_t, p->smem_t, c->stream>>>(a);
+	kern<<<grid, p->threads_t, p->smem_t, mgcu_stream()>>>(a);
 	MGCU_LAUNCHED();
-	if (p->ktime) { MGCU_TRY(cudaEventRecord(p->kev[p->kev_used + 1], c->stream)); p->kev_used += 2; }
+	if (p->ktime) { MGCU_TRY(cudaEventRecord(p->kev[p->kev_used + 1], mgcu_stream())); p->kev_used += 2; }
 	return 0;
 }
 
@@ -2224,7 +2382,22 @@ static int launch_columns(mgcu_plan* p, long b0, long b1, const typename P::T* d
 	if (!a.want_grad) a.cache = nullptr;
 	const long ncols = b1 - b0;
 	const int grid = (int)std::min<long>(p->grid_a, ncols);
-	k_columns<P, false><<<grid, p->threads, p->smem, c->stream>>>(a);
+	if (p->adj && p->adj_ok)
+	{
+		a.wmi = p->d_mats_inv.as<T>();
+		a.ck = p->ck.as<T>();
+		k_columns_adj<P><<<grid, ADJ_THREADS, p->smem, mgcu_stream()>>>(a);
+		MGCU_LAUNCHED();
+		return 0;
+	}
+	if (p->adj)
+	{
+		// gates that are not invertible: the cached sweep, its cache allocated on first need
+		const int e = p->cache.alloc((size_t)p->S * p->tsize * std::max(p->d.ngates, 1) * p->grid_a);
+		if (e) return e;
+		a.cache = p->cache.as<T>();
+	}
+	k_columns<P, false><<<grid, p->threads, p->smem, mgcu_stream()>>>(a);
 	MGCU_LAUNCHED();
 	if (p->d.want_hess)
 	{
@@ -2233,7 +2406,7 @@ static int launch_columns(mgcu_plan* p, long b0, long b1, const typename P::T* d
 		a.part_h = p->part_h.as<double>(); a.sh = p->sh.as<T>();
 		const long nitems = ncols * p->d.nplace * 8;
 		const int gb = (int)std::min<long>(p->grid_b, nitems);
-		k_hessian<P><<<gb, p->threads, p->smem, c->stream>>>(a, nitems);
+		k_hessian<P><<<gb, p->threads, p->smem, mgcu_stream()>>>(a, nitems);
 		MGCU_LAUNCHED();
 	}
 	return 0;
@@ -2244,6 +2417,7 @@ static int set_smem_attr()
 {
 	MgcuContext* c = mgcu_ctx();
 	MGCU_TRY(cudaFuncSetAttribute(k_columns<P, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)std::min<size_t>(c->smem_optin, 227 * 1024)));
+	MGCU_TRY(cudaFuncSetAttribute(k_columns_adj<P>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)std::min<size_t>(c->smem_optin, 227 * 1024)));
 	void (*const tk[10])(Args<P>) = { k_target<P, 256, 4>, k_target<P, 256, 8>, k_target<P, 256, 0>, k_target<P, 512, 2>,
 		k_target<P, 512, 4>, k_target<P, 512, 0>, k_target2<P, 4>, k_target2<P, 8>, k_target2<P, 0>, k_target<P, 128, 8> };
 	for (auto k : tk) MGCU_TRY(cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)std::min<size_t>(c->smem_optin, 227 * 1024)));
@@ -2253,15 +2427,17 @@ static int set_smem_attr()
 }
 
 template <class P>
-static int occupancy(int threads, size_t smem, int kt_t, int threads_t, int nc_t, size_t smem_t, bool w_t, int& per_sm, int& per_sm_target)
+static int occupancy(int threads, size_t smem, int kt_t, int threads_t, int nc_t, size_t smem_t, bool w_t, bool adj, int& per_sm,
+	int& per_sm_target)
 {
 	int n1 = 0, n2 = 0, n3 = 0;
-	MGCU_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n1, k_columns<P, false>, threads, smem));
+	if (adj) MGCU_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n1, k_columns_adj<P>, ADJ_THREADS, smem));
+	else MGCU_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n1, k_columns<P, false>, threads, smem));
 	MGCU_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n2, k_hessian<P>, threads, smem));
 	void (*kern)(Args<P>) = w_t ? k_target_w<P> : target_kernel<P>(kt_t, threads_t, nc_t);
 	if (!kern) { mg_set_error("no target-sweep kernel for 2^%d amplitudes and %d threads", kt_t, threads_t); return MG_ERR_ARG; }
 	MGCU_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n3, kern, threads_t, smem_t));
-	per_sm = std::max(1, std::min(n1, n2));
+	per_sm = std::max(1, adj ? n1 : std::min(n1, n2));   // gradient plans launch no Hessian items
 	per_sm_target = std::max(1, n3);
 	return 0;
 }
@@ -2297,26 +2473,39 @@ extern "C" mgcu_plan* mgcu_plan_create(const mgcu_plan_desc* d)
 	p->prec = d->precision;
 	p->tsize = prec_tsize(p->prec);
 
-	// tile size: 64 KB of state by default (2^12 complex of 16 B, 2^13 of 8 B)
+	// gradient plans: the checkpointed sweep (k_columns_adj, no per-gate cache) when
+	// FIT_CACHE = 2 asks for it (memory: one state per pass and block instead of one per gate);
+	// otherwise the cache, which measured faster in float-float (L=16, 40 gates: 1.29 s against
+	// 1.58 s per evaluation; L=18, 63 gates, even with the cache's grid cap: 1.43 s against
+	// 1.79 s per 4096 columns): the inverses add a third to the backward sweep's arithmetic,
+	// and the float-float sweeps are arithmetic-bound more than bound by the cache reads
+	p->adj = d->want_grad && !d->want_hess && mgcu_option(MG_OPT_FIT_CACHE_ID) == 2;
+	// tile size: 64 KB of state by default (2^12 complex of 16 B, 2^13 of 8 B); two tiles of
+	// 32 KB for the checkpointed sweep
 	int kt = (p->tsize == 16) ? 12 : 13;
+	if (p->adj) kt--;
 	const long opt_kt = mgcu_option(MG_OPT_TILE_BITS_ID);
 	if (opt_kt > 0) kt = (int)opt_kt;
 	kt = std::max(5, std::min(kt, MAXKT));   // >= 5: any gate fits beside the 3 fixed low bits
-	while (kt > 5 && ((size_t)1 << kt) * p->tsize > 200 * 1024) kt--;
+	while (kt > 5 && ((size_t)(p->adj ? 2 : 1) << kt) * p->tsize > 200 * 1024) kt--;
 	p->kt = std::min(kt, p->nb);
 	const int Q = 1 << (p->kt - 2);
 	int threads = std::max(32, std::min(256, Q));
 	const long opt_thr = mgcu_option(MG_OPT_THREADS_ID);
 	if (opt_thr > 0) threads = (int)std::max(32L, std::min(256L, (opt_thr / 32) * 32));
 	p->threads = threads;
-	// tile, deposit tables, reduction scratch
-	p->smem = ((size_t)1 << p->kt) * p->tsize + 2 * 128 * sizeof(unsigned) + red_bytes(threads);
+	// tile(s), deposit tables, reduction scratch (for the block size of the kernel that runs:
+	// k_columns_adj always launches ADJ_THREADS threads, more than `threads` for small tiles)
+	p->smem = ((size_t)(p->adj ? 2 : 1) << p->kt) * p->tsize + 2 * 128 * sizeof(unsigned)
+		+ red_bytes(p->adj ? std::max(threads, ADJ_THREADS) : threads);
 
 	schedule(p->L, p->kt, p->wires.data(), d->ngates, false, p->ws);
 
-	// the target sweep's own tile and block size (circuit targets only)
+	// the target sweep's own tile and block size (circuit targets only): by default 64 KB of
+	// state (as TILE_BITS), independent of the fitted circuit's tile (smaller for the
+	// checkpointed gradient sweep)
 	{
-		int ktt = p->kt;
+		int ktt = opt_kt > 0 ? (int)std::max(5L, std::min<long>(opt_kt, MAXKT)) : (p->tsize == 16 ? 12 : 13);
 		const long o = mgcu_option(MG_OPT_TARGET_TILE_BITS_ID);
 		if (o > 0) ktt = (int)std::max(5L, std::min<long>(o, MAXKT));
 		while (ktt > 5 && ((size_t)1 << ktt) * p->tsize > 128 * 1024) ktt--;
@@ -2357,9 +2546,9 @@ extern "C" mgcu_plan* mgcu_plan_create(const mgcu_plan_desc* d)
 			+ (p->w_t ? wtab_bytes(p->kt_t, p->maxg_t) : 0);
 	}
 	int per_sm = 1, per_sm_t = 1, e = 0;
-	if (p->prec == MG_PREC_FP64_ID) { e = set_smem_attr<PrecD>(); if (!e) e = occupancy<PrecD>(threads, p->smem, p->kt_t, p->threads_t, p->nc_t, p->smem_t, p->w_t, per_sm, per_sm_t); }
-	else if (p->prec == MG_PREC_FP32_ID) { e = set_smem_attr<PrecF>(); if (!e) e = occupancy<PrecF>(threads, p->smem, p->kt_t, p->threads_t, p->nc_t, p->smem_t, p->w_t, per_sm, per_sm_t); }
-	else { e = set_smem_attr<PrecX>(); if (!e) e = occupancy<PrecX>(threads, p->smem, p->kt_t, p->threads_t, p->nc_t, p->smem_t, p->w_t, per_sm, per_sm_t); }
+	if (p->prec == MG_PREC_FP64_ID) { e = set_smem_attr<PrecD>(); if (!e) e = occupancy<PrecD>(threads, p->smem, p->kt_t, p->threads_t, p->nc_t, p->smem_t, p->w_t, p->adj, per_sm, per_sm_t); }
+	else if (p->prec == MG_PREC_FP32_ID) { e = set_smem_attr<PrecF>(); if (!e) e = occupancy<PrecF>(threads, p->smem, p->kt_t, p->threads_t, p->nc_t, p->smem_t, p->w_t, p->adj, per_sm, per_sm_t); }
+	else { e = set_smem_attr<PrecX>(); if (!e) e = occupancy<PrecX>(threads, p->smem, p->kt_t, p->threads_t, p->nc_t, p->smem_t, p->w_t, p->adj, per_sm, per_sm_t); }
 	if (e) { delete p; return nullptr; }
 	const long opt_cps = mgcu_option(MG_OPT_CTAS_PER_SM_ID);
 	if (opt_cps > 0) per_sm = (int)std::min<long>(per_sm, opt_cps);
@@ -2393,7 +2582,8 @@ extern "C" mgcu_plan* mgcu_plan_create(const mgcu_plan_desc* d)
 	if (!e) e = upload_sched(p->ws, p->d_pass, p->d_gate);
 	if (!e) e = p->su.alloc(col_bytes * grid);
 	if (!e) e = p->sw.alloc(col_bytes * grid);
-	if (!e && grad) e = p->cache.alloc(col_bytes * ng * (d->want_hess ? chunk : grid));
+	if (!e && grad && !p->adj) e = p->cache.alloc(col_bytes * ng * (d->want_hess ? chunk : grid));
+	if (!e && p->adj) e = p->ck.alloc(col_bytes * p->ws.pass.size() * grid);
 	if (!e && d->want_hess) e = p->dcache.alloc(col_bytes * ng * chunk);
 	if (!e && d->want_hess) e = p->sh.alloc(col_bytes * p->grid_b);
 	if (!e) e = p->part_f.alloc(sizeof(double) * 2 * grid);
@@ -2410,7 +2600,7 @@ extern "C" mgcu_plan* mgcu_plan_create(const mgcu_plan_desc* d)
 	if (!e && d->want_hess) e = p->d_place.alloc(sizeof(int) * std::max(d->nplace, 1));
 	if (!e && d->want_hess) e = p->d_placew.alloc(sizeof(double) * std::max<size_t>((size_t)d->nplace * ng, 1));
 	if (e) { delete p; return nullptr; }
-	cudaStream_t st = c->stream;
+	cudaStream_t st = mgcu_stream();
 	bool ok = cudaMemcpyAsync(p->d_block.p, p->block.data(), sizeof(int) * ng, cudaMemcpyHostToDevice, st) == cudaSuccess;
 	ok = ok && cudaMemcpyAsync(p->d_pass_of.p, p->ws.pass_of.data(), sizeof(int) * d->ngates, cudaMemcpyHostToDevice, st) == cudaSuccess;
 	if (d->want_hess)
@@ -2429,14 +2619,18 @@ extern "C" long mgcu_plan_chunk_columns(const mgcu_plan* p) { return p->chunk; }
 
 extern "C" int mgcu_plan_set_gates(mgcu_plan* p, const mgg* gates)
 {
-	if (p->prec == MG_PREC_FP64_ID) return upload_mats<PrecD>(gates, p->d.ngates, p->d_mats);
-	if (p->prec == MG_PREC_FP32_ID) return upload_mats<PrecF>(gates, p->d.ngates, p->d_mats);
-	return upload_mats<PrecX>(gates, p->d.ngates, p->d_mats);
+	int e;
+	if (p->prec == MG_PREC_FP64_ID) e = upload_mats<PrecD>(gates, p->d.ngates, p->d_mats);
+	else if (p->prec == MG_PREC_FP32_ID) e = upload_mats<PrecF>(gates, p->d.ngates, p->d_mats);
+	else e = upload_mats<PrecX>(gates, p->d.ngates, p->d_mats);
+	if (e || !p->adj) return e;
+	if (p->prec == MG_PREC_FP32_ID) return upload_inverses<PrecF>(gates, p->d.ngates, p->d_mats_inv, p->adj_ok);
+	return upload_inverses<PrecX>(gates, p->d.ngates, p->d_mats_inv, p->adj_ok);
 }
 
 extern "C" int mgcu_plan_begin(mgcu_plan* p)
 {
-	cudaStream_t st = mgcu_ctx()->stream;
+	cudaStream_t st = mgcu_stream();
 	MGCU_TRY(cudaMemsetAsync(p->part_f.p, 0, p->part_f.n, st));
 	MGCU_TRY(cudaMemsetAsync(p->part_g.p, 0, p->part_g.n, st));
 	if (p->d.want_hess) MGCU_TRY(cudaMemsetAsync(p->part_h.p, 0, p->part_h.n, st));
@@ -2457,14 +2651,14 @@ static int plan_columns_t(mgcu_plan* p, long b0, long b1, const mgc* host_cols)
 		long dense_b0 = c0;
 		if (!t)
 		{
-			MGCU_TRY(cudaMemcpyAsync(p->cols64.p, host_cols + (size_t)(c0 - b0) * p->S, sizeof(double2) * n, cudaMemcpyHostToDevice, c->stream));
-			k_convert<P><<<grid_cap(n, 256), 256, 0, c->stream>>>(p->cols64.as<double2>(), n, p->cols.as<T>());
+			MGCU_TRY(cudaMemcpyAsync(p->cols64.p, host_cols + (size_t)(c0 - b0) * p->S, sizeof(double2) * n, cudaMemcpyHostToDevice, mgcu_stream()));
+			k_convert<P><<<grid_cap(n, 256), 256, 0, mgcu_stream()>>>(p->cols64.as<double2>(), n, p->cols.as<T>());
 			MGCU_LAUNCHED();
 			dense = p->cols.as<T>();
 		}
 		else if (t->kind == 1)
 		{
-			k_dense_columns<P><<<grid_cap(n, 256), 256, 0, c->stream>>>(t->dense.as<double2>(), p->L, c0, c1, p->cols.as<T>());
+			k_dense_columns<P><<<grid_cap(n, 256), 256, 0, mgcu_stream()>>>(t->dense.as<double2>(), p->L, c0, c1, p->cols.as<T>());
 			MGCU_LAUNCHED();
 			dense = p->cols.as<T>();
 		}
@@ -2506,7 +2700,7 @@ extern "C" int mgcu_plan_columns(mgcu_plan* p, long b0, long b1, const mgc* host
 extern "C" int mgcu_plan_finish(mgcu_plan* p)
 {
 	MgcuContext* c = mgcu_ctx();
-	cudaStream_t st = c->stream;
+	cudaStream_t st = mgcu_stream();
 	const int ng = std::max(p->d.ngates, 1);
 	k_sum_parts<<<1, 32, 0, st>>>(p->part_f.as<double>(), p->grid_a, 2, p->out_f.as<double>());
 	MGCU_LAUNCHED();
@@ -2532,7 +2726,7 @@ extern "C" int mgcu_plan_finish(mgcu_plan* p)
 
 extern "C" int mgcu_plan_fetch(mgcu_plan* p, mgc* f, mgg* dblocks, mgc* hess)
 {
-	cudaStream_t st = mgcu_ctx()->stream;
+	cudaStream_t st = mgcu_stream();
 	if (f) MGCU_TRY(cudaMemcpyAsync(f, p->out_f.p, sizeof(double) * 2, cudaMemcpyDeviceToHost, st));
 	if (dblocks && (p->d.want_grad || p->d.want_hess))
 		MGCU_TRY(cudaMemcpyAsync(dblocks, p->out_blk.p, sizeof(double) * 16 * p->d.nblocks, cudaMemcpyDeviceToHost, st));
@@ -2561,10 +2755,10 @@ extern "C" double mgcu_plan_time_ms(mgcu_plan* p, long b0, long b1, int steps, i
 	double total = 0;
 	for (int s = 0; s < steps; s++)
 	{
-		if (flush_l2 && cudaMemsetAsync(p->flush.p, s & 0xff, p->flush.n, c->stream) != cudaSuccess) return -1;
-		cudaEventRecord(c->ev0, c->stream);
+		if (flush_l2 && cudaMemsetAsync(p->flush.p, s & 0xff, p->flush.n, mgcu_stream()) != cudaSuccess) return -1;
+		cudaEventRecord(c->ev0, mgcu_stream());
 		if (mgcu_plan_begin(p) || mgcu_plan_columns(p, b0, b1, nullptr) || mgcu_plan_finish(p)) return -1;
-		cudaEventRecord(c->ev1, c->stream);
+		cudaEventRecord(c->ev1, mgcu_stream());
 		if (cudaEventSynchronize(c->ev1) != cudaSuccess) return -1;
 		float ms = 0;
 		cudaEventElapsedTime(&ms, c->ev0, c->ev1);
@@ -2708,9 +2902,9 @@ static double time_target(mgcu_target* t, int L, int kt, int threads, long ncols
 	double best = -1;
 	for (int rep = 0; rep < 2; rep++)
 	{
-		cudaEventRecord(c->ev0, c->stream);
-		kern<<<grid, threads, smem, c->stream>>>(a);
-		cudaEventRecord(c->ev1, c->stream);
+		cudaEventRecord(c->ev0, mgcu_stream());
+		kern<<<grid, threads, smem, mgcu_stream()>>>(a);
+		cudaEventRecord(c->ev1, mgcu_stream());
 		if (cudaEventSynchronize(c->ev1) != cudaSuccess) return -1;
 		float ms = 0;
 		cudaEventElapsedTime(&ms, c->ev0, c->ev1);
@@ -2921,7 +3115,7 @@ template <class P>
 static int batch_issue(mgcu_batch* B)
 {
 	typedef typename P::T T;
-	cudaStream_t st = mgcu_ctx()->stream;
+	cudaStream_t st = mgcu_stream();
 	MGCU_TRY(cudaMemsetAsync(B->parts.p, 0, B->parts.n, st));
 	MGCU_TRY(cudaMemsetAsync(B->counters.p, 0, B->counters.n, st));
 	const Args<P>* hat = reinterpret_cast<const Args<P>*>(B->host_args.data());
@@ -2964,7 +3158,7 @@ static int batch_issue(mgcu_batch* B)
 template <class P>
 static int batch_issue_graph(mgcu_batch* B)
 {
-	cudaStream_t st = mgcu_ctx()->stream;
+	cudaStream_t st = mgcu_stream();
 	if (!B->use_graph) return batch_issue<P>(B);
 	if (!B->exec)
 	{
@@ -3019,14 +3213,19 @@ extern "C" int mgcu_batch_set_gates(mgcu_batch* B, int i, const mgg* gates)
 }
 
 // one evaluation of every instance (graph replay; the first call captures the graph)
+// the batch's work queued on the calling thread's stream, without waiting for it
+extern "C" int mgcu_batch_issue(mgcu_batch* B)
+{
+	if (B->prec == MG_PREC_FP64_ID) return batch_issue_graph<PrecD>(B);
+	if (B->prec == MG_PREC_FP32_ID) return batch_issue_graph<PrecF>(B);
+	return batch_issue_graph<PrecX>(B);
+}
+
 extern "C" int mgcu_batch_run(mgcu_batch* B)
 {
-	int e;
-	if (B->prec == MG_PREC_FP64_ID) e = batch_issue_graph<PrecD>(B);
-	else if (B->prec == MG_PREC_FP32_ID) e = batch_issue_graph<PrecF>(B);
-	else e = batch_issue_graph<PrecX>(B);
+	const int e = mgcu_batch_issue(B);
 	if (e) return e;
-	MGCU_TRY(cudaStreamSynchronize(mgcu_ctx()->stream));
+	MGCU_TRY(cudaStreamSynchronize(mgcu_stream()));
 	return 0;
 }
 
@@ -3063,14 +3262,14 @@ extern "C" double mgcu_batch_time_ms(mgcu_batch* B, int steps, int flush_l2)
 	double total = 0;
 	for (int s = 0; s < steps; s++)
 	{
-		if (flush_l2 && cudaMemsetAsync(B->flush.p, s & 0xff, B->flush.n, c->stream) != cudaSuccess) return -1;
-		cudaEventRecord(c->ev0, c->stream);
+		if (flush_l2 && cudaMemsetAsync(B->flush.p, s & 0xff, B->flush.n, mgcu_stream()) != cudaSuccess) return -1;
+		cudaEventRecord(c->ev0, mgcu_stream());
 		int e;
 		if (B->prec == MG_PREC_FP64_ID) e = batch_issue_graph<PrecD>(B);
 		else if (B->prec == MG_PREC_FP32_ID) e = batch_issue_graph<PrecF>(B);
 		else e = batch_issue_graph<PrecX>(B);
 		if (e) return -1;
-		cudaEventRecord(c->ev1, c->stream);
+		cudaEventRecord(c->ev1, mgcu_stream());
 		if (cudaEventSynchronize(c->ev1) != cudaSuccess) return -1;
 		float ms = 0;
 		cudaEventElapsedTime(&ms, c->ev0, c->ev1);
@@ -3218,7 +3417,7 @@ extern "C" int mg_noalloc_brickwall_target_and_gradient(const void* ugates, int 
 		}
 	na_single_pass(L, na_wires_h, ng, 0, na_pass_h[0], na_gate_h);
 	na_single_pass(L, uwires, ungates, ng, na_pass_h[1], na_gate_h);
-	cudaStream_t st = c->stream;
+	cudaStream_t st = mgcu_stream();
 	const long ncols = 1L << L;
 	const int grid = (int)std::min<long>(NA_BLOCKS, ncols);
 	const int kt = L - 1;

@@ -177,7 +177,7 @@ int dev_apply(const mgg* g, int i, int j, int L, int ns, const double2* in, doub
 {
 	MgcuContext* c = mgcu_ctx();
 	const long nq = 1L << (L - 2);
-	k_apply<<<grid_for(nq * ns, 256), 256, 0, c->stream>>>(to_gate(g), L - 1 - i, L - 1 - j, L, ns, in, out);
+	k_apply<<<grid_for(nq * ns, 256), 256, 0, mgcu_stream()>>>(to_gate(g), L - 1 - i, L - 1 - j, L, ns, in, out);
 	MGCU_LAUNCHED();
 	return 0;
 }
@@ -189,9 +189,9 @@ int dev_backward(const mgg* g, int i, int j, int L, const double2* psi, const do
 	const int nb = grid_for(nq, 256);
 	int e = g_part.alloc(sizeof(double2) * 8 * nb);
 	if (e) return e;
-	k_backward<<<nb, 256, 0, c->stream>>>(to_gate(g), L - 1 - i, L - 1 - j, L, psi, dout, dpsi, g_part.as<double2>());
+	k_backward<<<nb, 256, 0, mgcu_stream()>>>(to_gate(g), L - 1 - i, L - 1 - j, L, psi, dout, dpsi, g_part.as<double2>());
 	MGCU_LAUNCHED();
-	k_sum_partials<<<1, 32, 0, c->stream>>>(g_part.as<double2>(), nb, 8, dg_dev);
+	k_sum_partials<<<1, 32, 0, mgcu_stream()>>>(g_part.as<double2>(), nb, 8, dg_dev);
 	MGCU_LAUNCHED();
 	return 0;
 }
@@ -204,9 +204,9 @@ int dev_backward_array(int i, int j, int L, int ns, const double2* psi, const do
 	if (nb > 64) nb = 64;
 	int e = g_part.alloc(sizeof(double2) * 8 * ns * nb);
 	if (e) return e;
-	k_backward_array<<<dim3(nb, ns), 128, 0, c->stream>>>(L - 1 - i, L - 1 - j, L, ns, psi, dout, g_part.as<double2>());
+	k_backward_array<<<dim3(nb, ns), 128, 0, mgcu_stream()>>>(L - 1 - i, L - 1 - j, L, ns, psi, dout, g_part.as<double2>());
 	MGCU_LAUNCHED();
-	k_sum_partials<<<1, 128, 0, c->stream>>>(g_part.as<double2>(), nb, 8 * ns, dg_dev);
+	k_sum_partials<<<1, 128, 0, mgcu_stream()>>>(g_part.as<double2>(), nb, 8 * ns, dg_dev);
 	MGCU_LAUNCHED();
 	return 0;
 }
@@ -215,19 +215,19 @@ int dev_placeholder(int i, int j, int L, int nout, const double2* psi, double2* 
 {
 	MgcuContext* c = mgcu_ctx();
 	const long nq = 1L << (L - 2);
-	k_placeholder<<<grid_for(nq, 128), 128, 0, c->stream>>>(L - 1 - i, L - 1 - j, L, nout, psi, out);
+	k_placeholder<<<grid_for(nq, 128), 128, 0, mgcu_stream()>>>(L - 1 - i, L - 1 - j, L, nout, psi, out);
 	MGCU_LAUNCHED();
 	return 0;
 }
 
 int sync_stream()
 {
-	MGCU_TRY(cudaStreamSynchronize(mgcu_ctx()->stream));
+	MGCU_TRY(cudaStreamSynchronize(mgcu_stream()));
 	return 0;
 }
 
-int h2d(void* dst, const void* src, size_t n) { MGCU_TRY(cudaMemcpyAsync(dst, src, n, cudaMemcpyHostToDevice, mgcu_ctx()->stream)); return 0; }
-int d2h(void* dst, const void* src, size_t n) { MGCU_TRY(cudaMemcpyAsync(dst, src, n, cudaMemcpyDeviceToHost, mgcu_ctx()->stream)); return 0; }
+int h2d(void* dst, const void* src, size_t n) { MGCU_TRY(cudaMemcpyAsync(dst, src, n, cudaMemcpyHostToDevice, mgcu_stream())); return 0; }
+int d2h(void* dst, const void* src, size_t n) { MGCU_TRY(cudaMemcpyAsync(dst, src, n, cudaMemcpyDeviceToHost, mgcu_stream())); return 0; }
 
 void gate_from_dev(const double2* d, mgg* g)
 {
@@ -409,7 +409,7 @@ extern "C" int mgcu_brickwall_backward_hessian(const mgg* vlist, int nlayers, co
 			TRY(dev_backward(&vlist[l], perms[l * L + p], perms[l * L + p + 1], L, C + (size_t)k * n, G + (size_t)k * n, dst, dgd.as<double2>() + 8 * k));
 			k--;
 		}
-	MGCU_TRY(cudaMemsetAsync(hdev.p, 0, sizeof(double2) * 64 * nlayers * nlayers, c->stream));
+	MGCU_TRY(cudaMemsetAsync(hdev.p, 0, sizeof(double2) * 64 * nlayers * nlayers, mgcu_stream()));
 	double2* cur = t0.as<double2>();
 	double2* nxt = t1.as<double2>();
 	for (int i = 0; i < nlayers; i++)
@@ -432,7 +432,7 @@ extern "C" int mgcu_brickwall_backward_hessian(const mgg* vlist, int nlayers, co
 					if (ti) { mult = half; if (j == i) mult -= o; }
 					o++;
 					TRY(dev_backward_array(perms[j * L + s], perms[j * L + s + 1], L, 8, cur, G + (size_t)lidx * n, hblk.as<double2>()));
-					k_hess_accumulate<<<1, 64, 0, c->stream>>>(hblk.as<double2>(), nlayers, i, j, mult, hdev.as<double2>());
+					k_hess_accumulate<<<1, 64, 0, mgcu_stream()>>>(hblk.as<double2>(), nlayers, i, j, mult, hdev.as<double2>());
 					MGCU_LAUNCHED();
 					if (j < nlayers - 1 || s < L - 2)
 					{
@@ -444,9 +444,9 @@ extern "C" int mgcu_brickwall_backward_hessian(const mgg* vlist, int nlayers, co
 			}
 		}
 	}
-	k_hess_symmetrize<<<grid_for((long)64 * nlayers * nlayers, 256), 256, 0, c->stream>>>(nlayers, hdev.as<double2>());
+	k_hess_symmetrize<<<grid_for((long)64 * nlayers * nlayers, 256), 256, 0, mgcu_stream()>>>(nlayers, hdev.as<double2>());
 	MGCU_LAUNCHED();
-	k_hess_mirror<<<grid_for((long)64 * nlayers * nlayers, 256), 256, 0, c->stream>>>(nlayers, hdev.as<double2>());
+	k_hess_mirror<<<grid_for((long)64 * nlayers * nlayers, 256), 256, 0, mgcu_stream()>>>(nlayers, hdev.as<double2>());
 	MGCU_LAUNCHED();
 	TRY(d2h(dpsi, g_a.p, bytes));
 	TRY(d2h(hess, hdev.p, sizeof(double2) * 64 * nlayers * nlayers));

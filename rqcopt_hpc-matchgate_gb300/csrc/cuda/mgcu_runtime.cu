@@ -51,6 +51,41 @@ MgcuContext* mgcu_ctx()
 	return &g_ctx;
 }
 
+// the stream this host thread issues its work on: the library's stream, or one the thread
+// selected (mgcu_stream_set), so that two host threads can keep work in flight on the GPU
+// at the same time (each waits for its own stream outside the library lock)
+static thread_local cudaStream_t t_stream = nullptr;
+
+cudaStream_t mgcu_stream()
+{
+	if (t_stream) return t_stream;
+	MgcuContext* c = mgcu_ctx();
+	return c ? c->stream : nullptr;
+}
+
+extern "C" void* mgcu_stream_create(void)
+{
+	if (!mgcu_ctx()) return nullptr;
+	cudaStream_t s = nullptr;
+	if (cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking) != cudaSuccess) { mg_set_error("cannot create a CUDA stream"); return nullptr; }
+	return (void*)s;
+}
+
+extern "C" void mgcu_stream_set(void* s) { t_stream = (cudaStream_t)s; }
+
+extern "C" int mgcu_stream_sync(void)
+{
+	cudaStream_t s = mgcu_stream();
+	if (!s) return MG_ERR_DEVICE;
+	MGCU_TRY(cudaStreamSynchronize(s));
+	return 0;
+}
+
+extern "C" void mgcu_stream_destroy(void* s)
+{
+	if (s) cudaStreamDestroy((cudaStream_t)s);
+}
+
 void mgcu_count_launch(long n) { g_launches += n; }
 
 extern "C" long mgcu_launch_count(void) { return g_launches.load(); }

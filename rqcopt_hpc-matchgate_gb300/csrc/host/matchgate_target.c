@@ -491,7 +491,7 @@ static int brickwall_eval(linear_func ufunc, void* udata, const struct matchgate
 }
 
 static int circuit_eval(linear_func ufunc, void* udata, const struct matchgate gates[], int ngates, const int wires[], int L,
-	int want_grad, int want_hess, numeric* fval, struct matchgate* dgates, numeric* hess)
+	int want_grad, int want_hess, numeric* fval, struct matchgate* dgates, numeric* hess, double* grad_vec, double* H)
 {
 	int* blk = identity_blocks(ngates);
 	if (!blk) return MG_ERR_ALLOC;
@@ -499,7 +499,7 @@ static int circuit_eval(linear_func ufunc, void* udata, const struct matchgate g
 	memset(&q, 0, sizeof(q));
 	q.L = L; q.ngates = ngates; q.nblocks = ngates; q.gates = gates; q.wires = wires; q.block = blk;
 	q.want_grad = want_grad; q.want_hess = want_hess; q.b0 = 0; q.b1 = -1;
-	q.fval = fval; q.dblocks = dgates; q.hess = hess;
+	q.fval = fval; q.dblocks = dgates; q.hess = hess; q.vblocks = gates; q.grad_vec = grad_vec; q.H = H;
 	int rc = run_eval(ufunc, udata, &q);
 	free(blk);
 	return rc;
@@ -512,7 +512,7 @@ static int circuit_eval(linear_func ufunc, void* udata, const struct matchgate g
 int matchgate_circuit_unitary_target(linear_func ufunc, void* udata,
 	const struct matchgate gates[], const int ngates, const int wires[], const int nqubits, numeric* fval)
 {
-	return circuit_eval(ufunc, udata, gates, ngates, wires, nqubits, 0, 0, fval, NULL, NULL);
+	return circuit_eval(ufunc, udata, gates, ngates, wires, nqubits, 0, 0, fval, NULL, NULL, NULL, NULL);
 }
 
 int parallel_matchgate_circuit_unitary_target(linear_func ufunc, void* udata,
@@ -525,14 +525,30 @@ int matchgate_circuit_unitary_target_and_gradient(linear_func ufunc, void* udata
 	const struct matchgate gates[], const int ngates, const int wires[], const int nqubits,
 	numeric* fval, struct matchgate dgates[])
 {
-	return circuit_eval(ufunc, udata, gates, ngates, wires, nqubits, 1, 0, fval, dgates, NULL);
+	return circuit_eval(ufunc, udata, gates, ngates, wires, nqubits, 1, 0, fval, dgates, NULL, NULL, NULL);
 }
 
 int matchgate_circuit_unitary_target_gradient_hessian(linear_func ufunc, void* udata,
 	const struct matchgate gates[], const int ngates, const int wires[], const int nqubits,
 	numeric* fval, struct matchgate dgates[], numeric* hess)
 {
-	return circuit_eval(ufunc, udata, gates, ngates, wires, nqubits, 1, 1, fval, dgates, hess);
+	return circuit_eval(ufunc, udata, gates, ngates, wires, nqubits, 1, 1, fval, dgates, hess, NULL, NULL);
+}
+
+/* per-gate Riemannian forms: the projection of src/matchgate_target.c:877-973 with one
+ * parameter block per gate instead of per layer */
+int matchgate_circuit_unitary_target_and_projected_gradient(linear_func ufunc, void* udata,
+	const struct matchgate gates[], const int ngates, const int wires[], const int nqubits,
+	numeric* fval, double* grad_vec)
+{
+	return circuit_eval(ufunc, udata, gates, ngates, wires, nqubits, 1, 0, fval, NULL, NULL, grad_vec, NULL);
+}
+
+int matchgate_circuit_unitary_target_gradient_vector_hessian_matrix(linear_func ufunc, void* udata,
+	const struct matchgate gates[], const int ngates, const int wires[], const int nqubits,
+	numeric* fval, double* grad_vec, double* H)
+{
+	return circuit_eval(ufunc, udata, gates, ngates, wires, nqubits, 1, 1, fval, NULL, NULL, grad_vec, H);
 }
 
 int matchgate_brickwall_unitary_target(linear_func ufunc, void* udata,
@@ -602,7 +618,8 @@ struct mg_plan
 {
 	mgcu_plan* p;
 	seq_circuit s;
-	int nlayers, L;
+	int nlayers, L;             /* nlayers: parameter blocks (layers, or gates of a circuit plan) */
+	int circuit;                /* 1: one block per gate (mg_plan_circuit) */
 	struct matchgate* vlist;
 };
 
@@ -637,12 +654,56 @@ mg_plan* mg_plan_brickwall(linear_func ufunc, void* udata, const struct matchgat
 	return pl;
 }
 
+mg_plan* mg_plan_circuit(linear_func ufunc, void* udata, const struct matchgate gates[], int ngates, const int wires[],
+	int nqubits, int what)
+{
+	mg_target_handle* th = as_handle(ufunc, udata);
+	if (!th || th->L != nqubits)
+	{
+		mg_set_error("mg_plan_circuit needs a GPU target (mg_target_*) on the same qubits");
+		return NULL;
+	}
+	if (ngates < 1 || (what & MG_EVAL_TI))
+	{
+		mg_set_error("mg_plan_circuit: needs at least one gate; the translation-invariant Hessian is for brickwalls");
+		return NULL;
+	}
+	mg_plan* pl = calloc(1, sizeof(*pl));
+	if (!pl) return NULL;
+	pl->circuit = 1;
+	pl->nlayers = ngates; pl->L = nqubits;
+	pl->s.ngates = ngates;
+	pl->s.gates = malloc(sizeof(struct matchgate) * ngates);
+	pl->s.wires = malloc(sizeof(int) * 2 * ngates);
+	pl->s.block = identity_blocks(ngates);
+	pl->vlist = malloc(sizeof(struct matchgate) * ngates);
+	if (!pl->s.gates || !pl->s.wires || !pl->s.block || !pl->vlist) { mg_plan_free(pl); return NULL; }
+	memcpy(pl->s.wires, wires, sizeof(int) * 2 * ngates);
+	mgcu_plan_desc d;
+	memset(&d, 0, sizeof(d));
+	d.L = nqubits; d.ngates = ngates; d.wires = pl->s.wires; d.nblocks = ngates; d.block = pl->s.block;
+	d.want_grad = (what & 3) >= MG_EVAL_GRADIENT; d.want_hess = (what & 3) == MG_EVAL_HESSIAN;
+	d.target = th->dev; d.precision = mgcu_precision();
+	int* place = NULL;
+	double* w = NULL;
+	if (d.want_hess && make_placements(ngates, nqubits / 2, 0, &place, &w, &d.nplace)) { mg_plan_free(pl); return NULL; }
+	d.place = place; d.place_w = w;
+	mgcu_lock();
+	pl->p = mgcu_plan_create(&d);
+	mgcu_unlock();
+	free(place); free(w);
+	if (!pl->p || mg_plan_set_gates(pl, gates)) { mg_plan_free(pl); return NULL; }
+	return pl;
+}
+
 int mg_plan_set_gates(mg_plan* pl, const struct matchgate vlist[])
 {
 	const int half = pl->L / 2;
 	memcpy(pl->vlist, vlist, sizeof(struct matchgate) * pl->nlayers);
-	for (int i = 0; i < pl->nlayers; i++)
-		for (int p = 0; p < half; p++) pl->s.gates[i * half + p] = vlist[i];
+	if (pl->circuit) memcpy(pl->s.gates, vlist, sizeof(struct matchgate) * pl->nlayers);
+	else
+		for (int i = 0; i < pl->nlayers; i++)
+			for (int p = 0; p < half; p++) pl->s.gates[i * half + p] = vlist[i];
 	mgcu_lock();
 	int r = mgcu_plan_set_gates(pl->p, (const mgg*)pl->s.gates);
 	mgcu_unlock();

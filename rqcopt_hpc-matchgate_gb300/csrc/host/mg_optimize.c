@@ -8,7 +8,8 @@
  * (src/mg_brickwall_opt.c:99-122): target Re f, Riemannian gradient and Hessian
  * (src/matchgate_target.c:877-973), Steihaug tCG, retraction per layer, the rho test
  * (rho < 1/4 shrinks the radius by 4, rho > 3/4 on the boundary doubles it up to maxradius,
- * the step is taken when rho > rho_trust).
+ * the step is taken when rho > rho_trust).  mg_optimize_circuit runs the same loop on a
+ * general circuit with one parameter block per gate.
  */
 #include <complex.h>
 #include <math.h>
@@ -20,6 +21,15 @@
 #include "mg_gb300.h"
 #include "../mg_internal.h"
 
+/* the circuit the fit optimises: a brickwall (one gate per layer, perms) or a general
+ * circuit (one parameter block per gate, wires) */
+typedef struct
+{
+	int L, nblocks;
+	const int** perms;    /* brickwall: [nblocks][L] */
+	const int* wires;     /* circuit: [2 nblocks] */
+} fit_t;
+
 typedef struct { mg_plan* h; mg_plan* f; int prec; } plans_t;
 
 static void plans_free(plans_t* p)
@@ -29,14 +39,23 @@ static void plans_free(plans_t* p)
 	p->h = p->f = NULL;
 }
 
-static int plans_make(plans_t* p, void* target, const struct matchgate* v, int nl, int L, const int* perms[], int prec)
+static int plans_make(plans_t* p, void* target, const struct matchgate* v, const fit_t* fit, int prec)
 {
 	plans_free(p);
 	const int old = mg_get_precision();
 	mg_set_precision(prec);
-	const int ti = mgcu_option(MG_OPT_TRANSLATIONAL_INVARIANCE_ID) != 0;
-	p->h = mg_plan_brickwall(mg_target_apply, target, v, nl, L, perms, MG_EVAL_HESSIAN | (ti ? MG_EVAL_TI : 0));
-	p->f = p->h ? mg_plan_brickwall(mg_target_apply, target, v, nl, L, perms, MG_EVAL_TARGET) : NULL;
+	const int nl = fit->nblocks, L = fit->L;
+	if (fit->perms)
+	{
+		const int ti = mgcu_option(MG_OPT_TRANSLATIONAL_INVARIANCE_ID) != 0;
+		p->h = mg_plan_brickwall(mg_target_apply, target, v, nl, L, fit->perms, MG_EVAL_HESSIAN | (ti ? MG_EVAL_TI : 0));
+		p->f = p->h ? mg_plan_brickwall(mg_target_apply, target, v, nl, L, fit->perms, MG_EVAL_TARGET) : NULL;
+	}
+	else
+	{
+		p->h = mg_plan_circuit(mg_target_apply, target, v, nl, fit->wires, L, MG_EVAL_HESSIAN);
+		p->f = p->h ? mg_plan_circuit(mg_target_apply, target, v, nl, fit->wires, L, MG_EVAL_TARGET) : NULL;
+	}
 	mg_set_precision(old);
 	p->prec = prec;
 	return (p->h && p->f) ? 0 : MG_ERR_DEVICE;
@@ -62,15 +81,10 @@ static int eval_f(plans_t* p, const struct matchgate* v, double* f)
 	return rc;
 }
 
-int mg_optimize_brickwall(void* target, const struct matchgate vlist0[], int nlayers, int nqubits, const int* perms[],
-	const struct rtr_params* params, int niter, double refine_gnorm, double f_iter[], int prec_iter[],
-	struct matchgate vlist_out[])
+static int optimize(void* target, const struct matchgate vlist0[], const fit_t* fit, const struct rtr_params* params, int niter,
+	double refine_gnorm, double f_iter[], int prec_iter[], struct matchgate vlist_out[])
 {
-	if (!target || !vlist0 || nlayers < 1 || !perms || !params || niter < 0 || !f_iter || !vlist_out)
-	{
-		mg_set_error("mg_optimize_brickwall: bad arguments");
-		return MG_ERR_ARG;
-	}
+	const int nlayers = fit->nblocks;
 	const int n = 8 * nlayers;
 	struct matchgate* x = malloc(sizeof(struct matchgate) * nlayers);
 	struct matchgate* xn = malloc(sizeof(struct matchgate) * nlayers);
@@ -81,7 +95,7 @@ int mg_optimize_brickwall(void* target, const struct matchgate vlist0[], int nla
 	memcpy(x, vlist0, sizeof(struct matchgate) * nlayers);
 	plans_t pl = { 0 };
 	int prec = refine_gnorm > 0 ? MG_PREC_MIXED : MG_PREC_FP64;
-	int rc = plans_make(&pl, target, x, nlayers, nqubits, perms, prec);
+	int rc = plans_make(&pl, target, x, fit, prec);
 	double radius = params->radius_init;
 	for (int k = 0; k < niter && !rc; k++)
 	{
@@ -96,7 +110,7 @@ int mg_optimize_brickwall(void* target, const struct matchgate vlist0[], int nla
 			{
 				/* near convergence: complex128 from here on, this iterate re-evaluated */
 				prec = MG_PREC_FP64;
-				rc = plans_make(&pl, target, x, nlayers, nqubits, perms, prec);
+				rc = plans_make(&pl, target, x, fit, prec);
 				if (!rc) rc = eval_hess(&pl, x, &fx, grad, H);
 				if (rc) break;
 			}
@@ -130,4 +144,32 @@ int mg_optimize_brickwall(void* target, const struct matchgate vlist0[], int nla
 	plans_free(&pl);
 	free(x); free(xn); free(grad); free(H); free(eta);
 	return rc;
+}
+
+int mg_optimize_brickwall(void* target, const struct matchgate vlist0[], int nlayers, int nqubits, const int* perms[],
+	const struct rtr_params* params, int niter, double refine_gnorm, double f_iter[], int prec_iter[],
+	struct matchgate vlist_out[])
+{
+	if (!target || !vlist0 || nlayers < 1 || !perms || !params || niter < 0 || !f_iter || !vlist_out)
+	{
+		mg_set_error("mg_optimize_brickwall: bad arguments");
+		return MG_ERR_ARG;
+	}
+	const fit_t fit = { nqubits, nlayers, perms, NULL };
+	return optimize(target, vlist0, &fit, params, niter, refine_gnorm, f_iter, prec_iter, vlist_out);
+}
+
+/* the same loop with one parameter block per gate of a general circuit: the per-gate
+ * Riemannian gradient and Hessian (8 ngates real parameters), retraction per gate */
+int mg_optimize_circuit(void* target, const struct matchgate gates0[], int ngates, const int wires[], int nqubits,
+	const struct rtr_params* params, int niter, double refine_gnorm, double f_iter[], int prec_iter[],
+	struct matchgate gates_out[])
+{
+	if (!target || !gates0 || ngates < 1 || !wires || !params || niter < 0 || !f_iter || !gates_out)
+	{
+		mg_set_error("mg_optimize_circuit: bad arguments");
+		return MG_ERR_ARG;
+	}
+	const fit_t fit = { nqubits, ngates, NULL, wires };
+	return optimize(target, gates0, &fit, params, niter, refine_gnorm, f_iter, prec_iter, gates_out);
 }

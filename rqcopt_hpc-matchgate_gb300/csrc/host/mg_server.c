@@ -26,6 +26,7 @@
 #include "trust_region.h"
 #include "mg_gb300.h"
 #include "mg_host.h"
+#include "../mg_internal.h"
 
 enum { ST_QUEUED = 0, ST_RUNNING = 1, ST_DONE = 2 };
 
@@ -45,17 +46,40 @@ typedef struct
 	long step;
 } req_t;
 
+/* a device-resident plan kept by the plan lane for later requests of the same shape */
+typedef struct
+{
+	void* target;
+	int L, nlayers, what;
+	int* perms;
+	mg_plan* plan;
+	size_t bytes;
+	long used;
+} pcache_t;
+
+#define NPCACHE 6
+
 struct mg_server
 {
 	pthread_mutex_t mu;
-	pthread_cond_t cv_work, cv_done;
-	pthread_t worker;
-	int stop, started;
+	pthread_cond_t cv_work, cv_done, cv_lane;
+	pthread_t worker, lane;
+	int stop, started, lane_started;
+	int lane_stop;                 /* set once the worker has exited */
 	size_t budget, peak;
 	int max_batch;
 	req_t** reqs;
 	long nreq, cap, next_queued;   /* next_queued: lowest id that may still be queued */
 	long steps, batched;
+	/* the plan lane: a second thread that serves a step's Hessian and trust-region-step
+	 * requests on its own stream while the worker's batch of f / gradient requests runs on
+	 * the library's stream, so the two overlap on the GPU */
+	req_t** lane_reqs;
+	int lane_n, lane_pending;
+	void* lane_stream;
+	pcache_t cache[NPCACHE];
+	long cache_clock;
+	size_t cache_bytes;
 };
 
 static double now_s(void)
@@ -102,24 +126,81 @@ static const int** perm_rows(const req_t* r, const int** rows)
 	return rows;
 }
 
-/* f, projected gradient and Hessian (what = MG_EVAL_*) of r's current gates on a plan */
-static int eval_plan(req_t* r, int what, double* f, double* grad_vec, double* H)
+/* the lane's plan for r's shape (target, qubits, layers, wiring, what): a cached one, or a
+ * new one kept while the cached plans stay within a quarter of the HBM budget (freeing a
+ * plan waits for the whole device, so the lane keeps recent ones) */
+static mg_plan* lane_plan(mg_server* sv, const req_t* r, int what)
 {
+	const size_t pb = sizeof(int) * (size_t)r->nlayers * r->L;
+	for (int i = 0; i < NPCACHE; i++)
+	{
+		pcache_t* c = &sv->cache[i];
+		if (c->plan && c->target == r->target && c->L == r->L && c->nlayers == r->nlayers && c->what == what && !memcmp(c->perms, r->perms, pb))
+		{
+			c->used = ++sv->cache_clock;
+			return c->plan;
+		}
+	}
 	const int** rows = malloc(sizeof(int*) * r->nlayers);
-	if (!rows) return MG_ERR_ALLOC;
+	if (!rows) return NULL;
 	mg_plan* pl = mg_plan_brickwall(mg_target_apply, r->target, r->vlist, r->nlayers, r->L, perm_rows(r, rows), what);
 	free(rows);
+	if (!pl) return NULL;
+	const size_t bytes = r->est;
+	/* evict least recently used plans until this one fits the slots and the byte cap */
+	for (;;)
+	{
+		int nused = 0, lru = -1;
+		for (int i = 0; i < NPCACHE; i++)
+			if (sv->cache[i].plan) { nused++; if (lru < 0 || sv->cache[i].used < sv->cache[lru].used) lru = i; }
+		if (nused < NPCACHE && sv->cache_bytes + bytes <= sv->budget / 4) break;
+		if (lru < 0) break;
+		mg_plan_free(sv->cache[lru].plan);
+		free(sv->cache[lru].perms);
+		sv->cache_bytes -= sv->cache[lru].bytes;
+		memset(&sv->cache[lru], 0, sizeof(pcache_t));
+	}
+	for (int i = 0; i < NPCACHE; i++)
+	{
+		pcache_t* c = &sv->cache[i];
+		if (c->plan) continue;
+		if (sv->cache_bytes + bytes > sv->budget / 4) break;
+		c->perms = malloc(pb);
+		if (!c->perms) break;
+		memcpy(c->perms, r->perms, pb);
+		c->target = r->target; c->L = r->L; c->nlayers = r->nlayers; c->what = what; c->plan = pl; c->bytes = bytes;
+		c->used = ++sv->cache_clock;
+		sv->cache_bytes += bytes;
+		return pl;
+	}
+	return pl;   /* not cached: the caller frees it */
+}
+
+static int lane_cached(const mg_server* sv, const mg_plan* pl)
+{
+	for (int i = 0; i < NPCACHE; i++) if (sv->cache[i].plan == pl) return 1;
+	return 0;
+}
+
+/* f, projected gradient and Hessian (what = MG_EVAL_*) of r's current gates on a lane plan;
+ * the wait for the GPU happens outside the library lock, so the worker's batch can be
+ * issued and collected meanwhile */
+static int eval_plan(mg_server* sv, req_t* r, int what, double* f, double* grad_vec, double* H)
+{
+	mg_plan* pl = lane_plan(sv, r, what);
 	if (!pl) return MG_ERR_DEVICE;
-	int rc = mg_plan_run(pl);
+	int rc = mg_plan_set_gates(pl, r->vlist);
+	if (!rc) rc = mg_plan_run(pl);
+	if (!rc) rc = mgcu_stream_sync();
 	numeric fc = 0;
 	if (!rc) rc = mg_plan_results(pl, &fc, NULL, NULL, grad_vec, H);
-	mg_plan_free(pl);
+	if (!lane_cached(sv, pl)) mg_plan_free(pl);
 	if (!rc) { f[0] = creal(fc); f[1] = cimag(fc); }
 	return rc;
 }
 
 /* one Riemannian trust-region step (the loop body of src/trust_region.c:258-305) */
-static int tr_step(req_t* r)
+static int tr_step(mg_server* sv, req_t* r)
 {
 	const int n = 8 * r->nlayers;
 	double f0[2], f1[2];
@@ -128,7 +209,7 @@ static int tr_step(req_t* r)
 	struct matchgate* vnew = malloc(sizeof(struct matchgate) * r->nlayers);
 	struct matchgate* vold = r->vlist;
 	int rc = (!eta || !heta || !vnew) ? MG_ERR_ALLOC : 0;
-	if (!rc) rc = eval_plan(r, MG_EVAL_HESSIAN, f0, r->grad_vec, r->H);
+	if (!rc) rc = eval_plan(sv, r, MG_EVAL_HESSIAN, f0, r->grad_vec, r->H);
 	if (!rc)
 	{
 		struct rtr_params rp;
@@ -146,7 +227,7 @@ static int tr_step(req_t* r)
 			eh += eta[i] * s;
 		}
 		r->vlist = vnew;
-		rc = eval_plan(r, MG_EVAL_TARGET, f1, NULL, NULL);
+		rc = eval_plan(sv, r, MG_EVAL_TARGET, f1, NULL, NULL);
 		r->vlist = vold;
 		if (!rc)
 		{
@@ -164,8 +245,11 @@ static int tr_step(req_t* r)
 	return rc;
 }
 
-/* the f / gradient requests of one step, as one batch */
-static void run_batch(req_t** rs, int n)
+/* the f / gradient requests of one step, as one batch on the library's stream: issued under
+ * the library lock, waited for outside it (the plan lane keeps issuing meanwhile), then
+ * collected.  Returns the batch, freed by the caller once the lane is idle (freeing device
+ * memory waits for the whole GPU). */
+static mgcu_batch* run_batch(req_t** rs, int n)
 {
 	mgcu_batch_inst* d = calloc(n, sizeof(mgcu_batch_inst));
 	seq_circuit* s = calloc(n, sizeof(seq_circuit));
@@ -190,7 +274,10 @@ static void run_batch(req_t** rs, int n)
 		b = mgcu_batch_create(n, d, mgcu_precision(), 0, 0);
 		rc = b ? 0 : MG_ERR_DEVICE;
 		for (int i = 0; i < n && !rc; i++) rc = mgcu_batch_set_gates(b, i, (const mgg*)s[i].gates);
-		if (!rc) rc = mgcu_batch_run(b);
+		if (!rc) rc = mgcu_batch_issue(b);
+		mgcu_unlock();
+		if (!rc) rc = mgcu_stream_sync();
+		mgcu_lock();
 		for (int i = 0; i < n && !rc; i++)
 		{
 			mgc f;
@@ -198,12 +285,59 @@ static void run_batch(req_t** rs, int n)
 			if (!rc) { rs[i]->f_re = f.re; rs[i]->f_im = f.im; }
 			if (!rc && rs[i]->kind == MG_REQ_GRADIENT) rc = mgcu_batch_project(b, i, (const mgg*)rs[i]->vlist, rs[i]->grad_vec);
 		}
-		if (b) mgcu_batch_destroy(b);
 		mgcu_unlock();
 	}
 	for (int i = 0; i < built; i++) seq_free(&s[i]);
 	for (int i = 0; i < n; i++) rs[i]->status = rc;
 	free(d); free(s);
+	return b;
+}
+
+/* mark r done (its results are in place) and wake the waiters */
+static void complete(mg_server* sv, req_t* r)
+{
+	pthread_mutex_lock(&sv->mu);
+	r->t_done = now_s();
+	r->state = ST_DONE;
+	pthread_cond_broadcast(&sv->cv_done);
+	pthread_mutex_unlock(&sv->mu);
+}
+
+/* the plan lane: serves the Hessian and trust-region-step requests each step hands it */
+static void* lane_worker(void* arg)
+{
+	mg_server* sv = (mg_server*)arg;
+	mgcu_stream_set(sv->lane_stream);
+	for (;;)
+	{
+		pthread_mutex_lock(&sv->mu);
+		while (!sv->lane_pending && !sv->lane_stop) pthread_cond_wait(&sv->cv_lane, &sv->mu);
+		if (!sv->lane_pending) { pthread_mutex_unlock(&sv->mu); break; }
+		req_t** rs = sv->lane_reqs;
+		const int n = sv->lane_n;
+		pthread_mutex_unlock(&sv->mu);
+		for (int i = 0; i < n; i++)
+		{
+			req_t* r = rs[i];
+			if (r->kind == MG_REQ_HESSIAN)
+			{
+				double f[2] = { 0, 0 };
+				r->status = eval_plan(sv, r, MG_EVAL_HESSIAN, f, r->grad_vec, r->H);
+				r->f_re = f[0]; r->f_im = f[1];
+			}
+			else r->status = tr_step(sv, r);
+			complete(sv, r);
+		}
+		pthread_mutex_lock(&sv->mu);
+		sv->lane_pending = 0;
+		pthread_cond_broadcast(&sv->cv_lane);
+		pthread_mutex_unlock(&sv->mu);
+	}
+	for (int i = 0; i < NPCACHE; i++)
+		if (sv->cache[i].plan) { mg_plan_free(sv->cache[i].plan); free(sv->cache[i].perms); }
+	memset(sv->cache, 0, sizeof(sv->cache));
+	mgcu_stream_set(NULL);
+	return NULL;
 }
 
 static void* worker(void* arg)
@@ -211,6 +345,7 @@ static void* worker(void* arg)
 	mg_server* sv = (mg_server*)arg;
 	req_t** step = malloc(sizeof(req_t*) * (size_t)sv->max_batch);
 	req_t** bat = malloc(sizeof(req_t*) * (size_t)sv->max_batch);
+	req_t** heavy = malloc(sizeof(req_t*) * (size_t)sv->max_batch);
 	for (;;)
 	{
 		pthread_mutex_lock(&sv->mu);
@@ -257,29 +392,28 @@ static void* worker(void* arg)
 		for (int i = 0; i < n; i++) { step[i]->state = ST_RUNNING; step[i]->t_start = t0; step[i]->step = stepno; }
 		pthread_mutex_unlock(&sv->mu);
 
-		int nb = 0;
+		int nb = 0, nh = 0;
 		for (int i = 0; i < n; i++)
 			if (step[i]->kind == MG_REQ_TARGET || step[i]->kind == MG_REQ_GRADIENT) bat[nb++] = step[i];
-		if (nb > 0) run_batch(bat, nb);
-		for (int i = 0; i < n; i++)
+			else heavy[nh++] = step[i];
+		if (nh > 0)
 		{
-			req_t* r = step[i];
-			if (r->kind == MG_REQ_HESSIAN)
-			{
-				double f[2];
-				r->status = eval_plan(r, MG_EVAL_HESSIAN, f, r->grad_vec, r->H);
-				r->f_re = f[0]; r->f_im = f[1];
-			}
-			else if (r->kind == MG_REQ_TRSTEP) r->status = tr_step(r);
+			/* the Hessian and trust-region-step requests go to the plan lane, which runs them
+			 * on its own stream while this thread's batch runs */
+			pthread_mutex_lock(&sv->mu);
+			sv->lane_reqs = heavy; sv->lane_n = nh; sv->lane_pending = 1;
+			pthread_cond_broadcast(&sv->cv_lane);
+			pthread_mutex_unlock(&sv->mu);
 		}
-		const double t1 = now_s();
+		mgcu_batch* b = nb > 0 ? run_batch(bat, nb) : NULL;
+		for (int i = 0; i < nb; i++) complete(sv, bat[i]);
 		pthread_mutex_lock(&sv->mu);
+		while (sv->lane_pending) pthread_cond_wait(&sv->cv_lane, &sv->mu);
 		sv->batched += nb;
-		for (int i = 0; i < n; i++) { step[i]->t_done = t1; step[i]->state = ST_DONE; }
-		pthread_cond_broadcast(&sv->cv_done);
 		pthread_mutex_unlock(&sv->mu);
+		if (b) { mgcu_lock(); mgcu_batch_destroy(b); mgcu_unlock(); }
 	}
-	free(step); free(bat);
+	free(step); free(bat); free(heavy);
 	return NULL;
 }
 
@@ -292,8 +426,24 @@ mg_server* mg_server_create(size_t hbm_budget_bytes, int max_batch)
 	pthread_mutex_init(&sv->mu, NULL);
 	pthread_cond_init(&sv->cv_work, NULL);
 	pthread_cond_init(&sv->cv_done, NULL);
+	pthread_cond_init(&sv->cv_lane, NULL);
+	sv->lane_stream = mgcu_stream_create();
+	if (!sv->lane_stream || pthread_create(&sv->lane, NULL, lane_worker, sv) != 0)
+	{
+		if (sv->lane_stream) mgcu_stream_destroy(sv->lane_stream);
+		mg_set_error("mg_server_create: could not start the plan lane (%s)", mg_last_error());
+		free(sv);
+		return NULL;
+	}
+	sv->lane_started = 1;
 	if (pthread_create(&sv->worker, NULL, worker, sv) != 0)
 	{
+		pthread_mutex_lock(&sv->mu);
+		sv->lane_stop = 1;
+		pthread_cond_broadcast(&sv->cv_lane);
+		pthread_mutex_unlock(&sv->mu);
+		pthread_join(sv->lane, NULL);
+		mgcu_stream_destroy(sv->lane_stream);
 		mg_set_error("mg_server_create: could not start the worker thread");
 		free(sv);
 		return NULL;
@@ -409,6 +559,16 @@ void mg_server_free(mg_server* sv)
 		pthread_mutex_unlock(&sv->mu);
 		pthread_join(sv->worker, NULL);
 	}
+	if (sv->lane_started)
+	{
+		/* after the worker: it may still hand the lane the requests it drains */
+		pthread_mutex_lock(&sv->mu);
+		sv->lane_stop = 1;
+		pthread_cond_broadcast(&sv->cv_lane);
+		pthread_mutex_unlock(&sv->mu);
+		pthread_join(sv->lane, NULL);
+		mgcu_stream_destroy(sv->lane_stream);
+	}
 	for (long i = 0; i < sv->nreq; i++)
 	{
 		req_t* r = sv->reqs[i];
@@ -417,6 +577,7 @@ void mg_server_free(mg_server* sv)
 	free(sv->reqs);
 	pthread_cond_destroy(&sv->cv_work);
 	pthread_cond_destroy(&sv->cv_done);
+	pthread_cond_destroy(&sv->cv_lane);
 	pthread_mutex_destroy(&sv->mu);
 	free(sv);
 }

@@ -36,9 +36,17 @@ extern "C" {
 #define MG_OPT_TRANSLATIONAL_INVARIANCE_ID 8
 #define MG_OPT_TARGET_DENSE_ID  9
 #define MG_OPT_HOST_THREADS_ID  10
-#define MG_NOPTIONS             10
+#define MG_OPT_FIT_CACHE_ID     11
+#define MG_NOPTIONS             11
 
 /* ---- runtime ---- */
+/* streams: each host thread issues its GPU work on its own stream when it selected one
+ * (mgcu_stream_set; NULL: the library's stream); mgcu_stream_sync waits for the calling
+ * thread's stream and needs no library lock */
+void* mgcu_stream_create(void);
+void mgcu_stream_set(void* stream);
+int mgcu_stream_sync(void);
+void mgcu_stream_destroy(void* stream);
 void mg_set_error(const char* fmt, ...);
 const char* mg_last_error(void);
 void mgcu_lock(void);
@@ -123,6 +131,7 @@ mgcu_batch* mgcu_batch_create(int n, const mgcu_batch_inst* insts, int precision
 void mgcu_batch_destroy(mgcu_batch* b);
 int mgcu_batch_set_gates(mgcu_batch* b, int i, const mgg* gates);   /* [ngates_i] */
 int mgcu_batch_run(mgcu_batch* b);
+int mgcu_batch_issue(mgcu_batch* b);     /* queued on the calling thread's stream, no wait */
 int mgcu_batch_fetch(mgcu_batch* b, int i, mgc* f, mgg* dblocks);
 int mgcu_batch_project(mgcu_batch* b, int i, const mgg* vblocks, double* grad_vec);
 int mgcu_batch_info(const mgcu_batch* b, int i, int* target_tile_bits, int* target_passes, int* items);

@@ -26,6 +26,7 @@ OPT_TARGET_TILE_BITS, OPT_TARGET_THREADS, OPT_TARGET_COLUMNS = 5, 6, 7
 OPT_TRANSLATIONAL_INVARIANCE = 8
 OPT_TARGET_DENSE = 9
 OPT_HOST_THREADS = 10
+OPT_FIT_CACHE = 11
 EVAL_TARGET, EVAL_GRADIENT, EVAL_HESSIAN, EVAL_TI = 0, 1, 2, 4
 
 P = C.c_void_p
@@ -250,6 +251,21 @@ class MatchgateLib:
             raise RuntimeError(self.last_error())
         return f_iter, prec, xf
 
+    def optimize_circuit_native(self, target, gates0, wires, L, niter, refine_gnorm=0.0, tcg_maxiter=None,
+                                rho_trust=0.125, radius_init=0.01, maxradius=0.1):
+        """mg_optimize_circuit (one parameter block per gate): (f_iter, prec_iter, final gates)"""
+        g0 = gates_arr(gates0); ng = len(g0)
+        w = np.ascontiguousarray(np.asarray(wires, np.int32).reshape(-1))
+        prm = RtrParams()
+        prm.tcg_params = TcgParams(tcg_maxiter if tcg_maxiter is not None else 2 * 8 * ng, 1e-8, 1e-6)
+        prm.rho_trust, prm.radius_init, prm.maxradius = rho_trust, radius_init, maxradius
+        f_iter = np.zeros(niter + 1); prec = np.zeros(niter + 1, np.int32); xf = np.zeros((ng, 8), cd)
+        rc = self.lib.mg_optimize_circuit(P(target), _p(g0), ng, _p(w), L, C.byref(prm), niter, C.c_double(refine_gnorm),
+                                          _p(f_iter), _p(prec), _p(xf))
+        if rc != 0:
+            raise RuntimeError(self.last_error())
+        return f_iter, prec, xf
+
     # ------------------------------------------------------------------ target construction
     def hubbard_trotter_circuit(self, nsites, J, U, t, nsteps, order=2):
         """(gates [n, 8], wires [n, 2]) of the Suzuki circuit built by the library"""
@@ -441,6 +457,20 @@ class MatchgateLib:
         f = np.zeros(1, cd); dg = np.zeros((len(g), 8), cd); m = 8 * len(g); h = np.zeros((m, m), cd)
         rc = self.lib.matchgate_circuit_unitary_target_gradient_hessian(P(ufunc), P(udata), _p(g), len(g), _p(w), L, _p(f), _p(dg), _p(h))
         return rc, f[0], dg, h
+
+    def circuit_gradvec_hessmat(self, ufunc, udata, gates, wires, L):
+        """per-gate Riemannian gradient [8 ngates] and Hessian [(8 ngates)^2]"""
+        g = gates_arr(gates); w = np.ascontiguousarray(np.asarray(wires, np.int32).reshape(-1))
+        f = np.zeros(1, cd); m = 8 * len(g); gv = np.zeros(m); H = np.zeros((m, m))
+        rc = self.lib.matchgate_circuit_unitary_target_gradient_vector_hessian_matrix(P(ufunc), P(udata), _p(g), len(g), _p(w), L,
+                                                                                     _p(f), _p(gv), _p(H))
+        return rc, f[0], gv, H
+
+    def circuit_projected_gradient(self, ufunc, udata, gates, wires, L):
+        g = gates_arr(gates); w = np.ascontiguousarray(np.asarray(wires, np.int32).reshape(-1))
+        f = np.zeros(1, cd); gv = np.zeros(8 * len(g))
+        rc = self.lib.matchgate_circuit_unitary_target_and_projected_gradient(P(ufunc), P(udata), _p(g), len(g), _p(w), L, _p(f), _p(gv))
+        return rc, f[0], gv
 
     def brickwall_target(self, ufunc, udata, vlist, perms, L):
         v = gates_arr(vlist); pp, rows = _perm_ptrs(perms, L); f = np.zeros(1, cd)
