@@ -419,6 +419,7 @@ def run_gb300(a):
         "roofline": {"bound": "fp32", "achieved": achieved, "peak": fp32_peak / 1e3, "unit": "TFLOP/s",
                      "frac": achieved / (fp32_peak / 1e3), "traffic": traffic,
                      "kernel": "k_target (target sweep)", "kernel_launches": tk_n,
+                     "kernel_config": lib.plan_target_config(plan),
                      "kernel_ms_per_launch": tk_avg_s * 1e3, "kernel_share_of_step": tk_ms / total_ms,
                      "columns_per_launch": cols_per_launch,
                      "achieved_is": "algorithmic complex-arithmetic flops of the target sweep (14 per visited "

@@ -51,11 +51,16 @@ int mg_get_precision(void);
  * are recovered with the gates' block inverses (one state per pass and block instead of one
  * per gate, much less device memory and traffic, but a third more arithmetic and about 25 %
  * slower in float-float at L=16-18; gates that are not invertible fall back to the cache).
- * Hessian evaluations always cache. */
+ * Hessian evaluations always cache.
+ * TARGET_TUNE: how the block size of a GPU circuit target's sweep is chosen when
+ * TARGET_THREADS is 0.  0 (default): by timing the candidates (128 or 256 threads, and for
+ * the full sweep 512) on one resident wave of columns when the trace has at least 2^14
+ * columns, once per target, precision and tile size; 1: never (128 threads); 2: always.
+ * The candidates give bit-identical results. */
 enum { MG_OPT_TILE_BITS = 1, MG_OPT_THREADS = 2, MG_OPT_CHUNK_COLUMNS = 3, MG_OPT_CTAS_PER_SM = 4,
        MG_OPT_TARGET_TILE_BITS = 5, MG_OPT_TARGET_THREADS = 6, MG_OPT_TARGET_COLUMNS = 7,
        MG_OPT_TRANSLATIONAL_INVARIANCE = 8, MG_OPT_TARGET_DENSE = 9, MG_OPT_HOST_THREADS = 10,
-       MG_OPT_FIT_CACHE = 11 };
+       MG_OPT_FIT_CACHE = 11, MG_OPT_TARGET_TUNE = 12 };
 int mg_set_option(int option, long value);
 long mg_get_option(int option);
 
@@ -255,6 +260,11 @@ double mg_plan_time_ms(mg_plan* plan, int steps, int flush_l2);
 /* The target-sweep kernel launches inside the last mg_plan_time_ms call (circuit
  * targets): their number and summed duration from CUDA events around each launch. */
 int mg_plan_target_kernel_ms(mg_plan* plan, double* ms, long* launches);
+/* The target sweep a plan runs: cfg[0] = 0 (no GPU sweep: dense target or host map), 1 (every
+ * amplitude) or 2 (weight-restricted); cfg[1] its tile bits; cfg[2] threads per block (as
+ * MG_OPT_TARGET_TUNE chose them); cfg[3] live quartets per thread and iteration
+ * (weight-restricted) or basis columns per block (every amplitude). */
+int mg_plan_target_config(const mg_plan* plan, int cfg[4]);
 /* Number of kernels this library has launched since it was loaded. */
 long mg_launch_count(void);
 /* Peak FP32 FMA rate of this GPU, measured by a dependent-FMA kernel of this library

@@ -989,8 +989,9 @@ __device__ __forceinline__ void tgt_quartets_w(unsigned tb, unsigned td, const T
 	else tgt_block<P, NQ, SG, 1>(tb, td, x, (unsigned)r.m.y, (unsigned)r.m.z, kw & 7, (kw >> 6) & 15, m, sg);
 }
 
-// one gate on the live quartets [j0, j1) of the popcount-sorted order, two per iteration
-template <class P, bool SG>
+// one gate on the live quartets [j0, j1) of the popcount-sorted order, NQ (1 or 2) per
+// iteration
+template <class P, bool SG, int NQ>
 __device__ __forceinline__ void tgt_gate_w(unsigned tb, unsigned td, const TGate& r, unsigned mats, int tpar, unsigned nlb,
 	const unsigned short* perm, unsigned j0, unsigned j1)
 {
@@ -998,13 +999,18 @@ __device__ __forceinline__ void tgt_gate_w(unsigned tb, unsigned td, const TGate
 	const unsigned m = mats + (unsigned)r.h.y * 8u * (unsigned)ES;
 	const unsigned sn = SG ? (unsigned)__popc(nlb & (unsigned)r.snl) : 0u;
 	unsigned j = j0 + threadIdx.x;
-	for (; j + blockDim.x < j1; j += 2 * blockDim.x) tgt_quartets_w<P, 2, SG>(tb, td, r, m, tpar, sn, perm, j, blockDim.x);
-	if (j < j1) tgt_quartets_w<P, 1, SG>(tb, td, r, m, tpar, sn, perm, j, blockDim.x);
+	if (NQ == 2)
+	{
+		for (; j + blockDim.x < j1; j += 2 * blockDim.x) tgt_quartets_w<P, 2, SG>(tb, td, r, m, tpar, sn, perm, j, blockDim.x);
+		if (j < j1) tgt_quartets_w<P, 1, SG>(tb, td, r, m, tpar, sn, perm, j, blockDim.x);
+	}
+	else
+		for (; j < j1; j += blockDim.x) tgt_quartets_w<P, 1, SG>(tb, td, r, m, tpar, sn, perm, j, blockDim.x);
 }
 
 // the gates [gbeg, gend) of a pass on one tile of nonlocal bits nlb, for a column of weight
 // wb; F free bits per quartet.  One barrier per gate that has live quartets in the tile.
-template <class P>
+template <class P, int NQ>
 __device__ __forceinline__ void tgt_gates_w(unsigned tb, unsigned td, const TGate* gates, int gbeg, int gend, unsigned mats,
 	int tpar, unsigned nlb, int wb, int F, const unsigned short* perm, const int* start)
 {
@@ -1015,8 +1021,8 @@ __device__ __forceinline__ void tgt_gates_w(unsigned tb, unsigned td, const TGat
 		if (!(r.act & 0x100)) continue;
 		const int rlo = max(0, delta + (r.act & 15) - 4), rhi = min(F, delta + ((r.act >> 4) & 15) - 4);
 		if (rlo > rhi) continue;   // no live quartet in this tile (the same for the whole block)
-		if (r.sl | r.snl) tgt_gate_w<P, true>(tb, td, r, mats, tpar, nlb, perm, (unsigned)start[rlo], (unsigned)start[rhi + 1]);
-		else tgt_gate_w<P, false>(tb, td, r, mats, tpar, nlb, perm, (unsigned)start[rlo], (unsigned)start[rhi + 1]);
+		if (r.sl | r.snl) tgt_gate_w<P, true, NQ>(tb, td, r, mats, tpar, nlb, perm, (unsigned)start[rlo], (unsigned)start[rhi + 1]);
+		else tgt_gate_w<P, false, NQ>(tb, td, r, mats, tpar, nlb, perm, (unsigned)start[rlo], (unsigned)start[rhi + 1]);
 		__syncthreads();
 	}
 }
@@ -1092,7 +1098,7 @@ __device__ __forceinline__ void tgt_column(const Args<P>& a, const long (&bs)[NC
 			}
 			__syncthreads();
 			if (W)
-				tgt_gates_w<P>(tb, td, reinterpret_cast<const TGate*>(smem_raw + a.wperm_off + wtab_rec_off(kt)), 0,
+				tgt_gates_w<P, QPT == 1 ? 1 : 2>(tb, td, reinterpret_cast<const TGate*>(smem_raw + a.wperm_off + wtab_rec_off(kt)), 0,
 					pr.gend - pr.gbeg, pms, tpar, nlb, __popcll(bs[0]), kt - 2,
 					reinterpret_cast<const unsigned short*>(smem_raw + a.wperm_off),
 					reinterpret_cast<const int*>(smem_raw + a.wperm_off + wtab_start_off(kt)));
@@ -1131,9 +1137,11 @@ __global__ void __launch_bounds__(NT, (NT == 512 && QPT == 4) ? 1 : (NT == 128 ?
 		tgt_column<P, QPT>(a, b, a.ucols + (size_t)(b - a.b0) * a.S, smem_raw);
 }
 
-// the weight-restricted sweep (targets that conserve the Hamming weight), 128 threads
-template <class P>
-__global__ void __launch_bounds__(128, 3) k_target_w(Args<P> a)
+// the weight-restricted sweep (targets that conserve the Hamming weight): NT threads, NQ
+// live quartets per thread and iteration, three blocks per SM: 128 x 2, or 256 x 1 (at most
+// 85 registers; more warps per SM, half the quartets in flight per thread)
+template <class P, int NT, int NQ>
+__global__ void __launch_bounds__(NT, 3) k_target_w(Args<P> a)
 {
 	extern __shared__ __align__(16) char smem_raw[];
 	w_perm_setup(a.kt - 2, reinterpret_cast<unsigned short*>(smem_raw + a.wperm_off),
@@ -1142,15 +1150,19 @@ __global__ void __launch_bounds__(128, 3) k_target_w(Args<P> a)
 	{
 		const long bs[1] = { b };
 		typename P::T* const outs[1] = { a.ucols + (size_t)(b - a.b0) * a.S };
-		tgt_column<P, 0, 1, true>(a, bs, outs, smem_raw);
+		tgt_column<P, NQ, 1, true>(a, bs, outs, smem_raw);
 	}
 }
 
-// bytes of k_target_w's tables after the staged matrices: the sorted free-bit values and
-// the popcount starts
 // bytes of k_target_w's tables after the staged matrices: the sorted free-bit values, the
 // popcount starts and the records of one pass (at most maxg gates)
 constexpr size_t wtab_bytes(int kt, int maxg) { return wtab_rec_off(kt) + (size_t)maxg * sizeof(TGate); }
+
+template <class P>
+static void (*w_kernel(int threads, int nq))(Args<P>)
+{
+	return (threads == 256 && nq == 1) ? k_target_w<P, 256, 1> : k_target_w<P, 128, 2>;
+}
 
 // two columns of equal parity per block (b, b ^ 3 within each aligned group of four),
 // sharing every per-gate computation; columns outside whole groups one at a time
@@ -1861,6 +1873,7 @@ struct mgcu_target
 	// the gate list the target sweep runs (fermionic swaps relabelled away, see
 	// relabel_fswaps) with per-gate Jordan-Wigner string wires
 	int tuned_kt[3][32] = {};      // batch tile choice per precision and L (0: not tuned yet)
+	std::map<std::array<int, 4>, std::array<int, 2>> tuned_sweep;   // plan sweep choice: (prec, tile bits, weight-restricted, 0) -> (threads, quartets)
 	bool sweep_ready = false;
 	std::vector<mgg> sg;
 	std::vector<int> sw;
@@ -2297,6 +2310,7 @@ struct mgcu_plan
 	int pm_cap = MAXPM;            // staged matrices per pass k_target has room for
 	bool w_t = false;              // the weight-restricted sweep (k_target_w)
 	int maxg_t = MAXPG;            // k_target_w: room for this many staged gate records
+	int nq_t = 2;                  // k_target_w: live quartets per thread and iteration
 	bool ktime = false;            // record events around k_target launches (mgcu_plan_time_ms)
 	std::vector<cudaEvent_t> kev;  // start/stop pairs
 	size_t kev_used = 0;
@@ -2316,6 +2330,15 @@ struct mgcu_plan
 };
 
 static size_t prec_tsize(int prec) { return prec == MG_PREC_FP32_ID ? 8 : 16; }
+
+// k_target's dynamic shared memory for tt threads: tile(s), deposit tables, reduction
+// scratch, the staged matrices and (weight-restricted sweep) its tables and records
+static size_t target_smem_bytes(const mgcu_plan* p, int tt)
+{
+	return (size_t)p->nc_t * ((size_t)1 << p->kt_t) * p->tsize + 2 * 128 * sizeof(unsigned)
+		+ std::max<size_t>((size_t)(tt / 32) * 16 * sizeof(double), 16 * 16) + (size_t)p->pm_cap * 8 * p->tsize
+		+ (p->w_t ? wtab_bytes(p->kt_t, p->maxg_t) : 0);
+}
 
 // -conj(U e_b) of a circuit target for b in [b0, b1) into out[b - b0]
 template <class P>
@@ -2350,7 +2373,7 @@ static int launch_target(mgcu_plan* p, long b0, long b1, typename P::T* out)
 			p->kev.push_back(ev);
 		}
 	if (p->ktime) MGCU_TRY(cudaEventRecord(p->kev[p->kev_used], mgcu_stream()));
-	void (*kern)(Args<P>) = p->w_t ? k_target_w<P> : target_kernel<P>(p->kt_t, p->threads_t, p->nc_t);
+	void (*kern)(Args<P>) = p->w_t ? w_kernel<P>(p->threads_t, p->nq_t) : target_kernel<P>(p->kt_t, p->threads_t, p->nc_t);
 	if (!kern) { mg_set_error("no target-sweep kernel for 2^%d amplitudes and %d threads", p->kt_t, p->threads_t); return MG_ERR_ARG; }
 	kern<<<grid, p->threads_t, p->smem_t, mgcu_stream()>>>(a);
 	MGCU_LAUNCHED();
@@ -2421,24 +2444,99 @@ static int set_smem_attr()
 	void (*const tk[10])(Args<P>) = { k_target<P, 256, 4>, k_target<P, 256, 8>, k_target<P, 256, 0>, k_target<P, 512, 2>,
 		k_target<P, 512, 4>, k_target<P, 512, 0>, k_target2<P, 4>, k_target2<P, 8>, k_target2<P, 0>, k_target<P, 128, 8> };
 	for (auto k : tk) MGCU_TRY(cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)std::min<size_t>(c->smem_optin, 227 * 1024)));
-	MGCU_TRY(cudaFuncSetAttribute(k_target_w<P>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)std::min<size_t>(c->smem_optin, 227 * 1024)));
+	void (*const wk[2])(Args<P>) = { k_target_w<P, 128, 2>, k_target_w<P, 256, 1> };
+	for (auto k : wk) MGCU_TRY(cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)std::min<size_t>(c->smem_optin, 227 * 1024)));
 	MGCU_TRY(cudaFuncSetAttribute(k_hessian<P>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)std::min<size_t>(c->smem_optin, 227 * 1024)));
 	return 0;
 }
 
 template <class P>
-static int occupancy(int threads, size_t smem, int kt_t, int threads_t, int nc_t, size_t smem_t, bool w_t, bool adj, int& per_sm,
+static int occupancy(int threads, size_t smem, int kt_t, int threads_t, int nc_t, size_t smem_t, bool w_t, int nq_t, bool adj, int& per_sm,
 	int& per_sm_target)
 {
 	int n1 = 0, n2 = 0, n3 = 0;
 	if (adj) MGCU_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n1, k_columns_adj<P>, ADJ_THREADS, smem));
 	else MGCU_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n1, k_columns<P, false>, threads, smem));
 	MGCU_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n2, k_hessian<P>, threads, smem));
-	void (*kern)(Args<P>) = w_t ? k_target_w<P> : target_kernel<P>(kt_t, threads_t, nc_t);
+	void (*kern)(Args<P>) = w_t ? w_kernel<P>(threads_t, nq_t) : target_kernel<P>(kt_t, threads_t, nc_t);
 	if (!kern) { mg_set_error("no target-sweep kernel for 2^%d amplitudes and %d threads", kt_t, threads_t); return MG_ERR_ARG; }
 	MGCU_TRY(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n3, kern, threads_t, smem_t));
 	per_sm = std::max(1, adj ? n1 : std::min(n1, n2));   // gradient plans launch no Hessian items
 	per_sm_target = std::max(1, n3);
+	return 0;
+}
+
+// The target sweep's block size, chosen by timing: each candidate (threads, and for the
+// weight-restricted sweep live quartets per thread and iteration) traces one resident wave
+// of columns twice with the plan's own program, and the faster second run wins.  Every
+// candidate applies the same operations to each amplitude in the same order, so the choice
+// changes the speed only, never a bit of a result; it is cached on the target per
+// precision, tile size and sweep kind.  The columns traced start at a third of the range,
+// where the column weights are typical of the whole.
+template <class P>
+static int tune_target_sweep(mgcu_plan* p)
+{
+	typedef typename P::T T;
+	MgcuContext* c = mgcu_ctx();
+	mgcu_target* t = p->d.target;
+	const std::array<int, 4> key = { p->prec, p->kt_t, p->w_t ? 1 : 0, 0 };
+	std::vector<std::array<int, 2>> cand;
+	auto it = t->tuned_sweep.find(key);
+	if (it != t->tuned_sweep.end()) cand.push_back(it->second);
+	else if (p->w_t) cand = { { 128, 2 }, { 256, 1 } };
+	else
+	{
+		const int Q = 1 << (p->kt_t - 2);
+		for (int th : { 128, 256, 512 })
+		{
+			const int q = Q / th;
+			if (Q % th == 0 && ((th == 128 && q == 8) || (th == 256 && (q == 4 || q == 8)) || (th == 512 && (q == 2 || q == 4))))
+				cand.push_back({ th, 2 });
+		}
+	}
+	if (cand.empty()) return 0;
+	int e = set_smem_attr<P>();
+	if (e) return e;
+	auto kernel_of = [&](const std::array<int, 2>& cd) {
+		return p->w_t ? w_kernel<P>(cd[0], cd[1]) : target_kernel<P>(p->kt_t, cd[0], 1);
+	};
+	std::array<int, 2> best = cand[0];
+	if (cand.size() > 1)
+	{
+		const long ncols = 1L << p->L;
+		DevBuf tmp;
+		if (tmp.alloc(sizeof(T) * (size_t)p->S * std::min<long>(ncols, (long)c->nsm * 4))) { cudaGetLastError(); return 0; }
+		cudaEvent_t ev[2];
+		MGCU_TRY(cudaEventCreate(&ev[0]));
+		if (cudaEventCreate(&ev[1]) != cudaSuccess) { cudaEventDestroy(ev[0]); return MG_ERR_DEVICE; }
+		float best_ms = -1;
+		for (const auto& cd : cand)
+		{
+			int per = 0;
+			const size_t sm = target_smem_bytes(p, cd[0]);
+			if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, kernel_of(cd), cd[0], sm) != cudaSuccess || per < 1) continue;
+			p->threads_t = cd[0]; p->nq_t = cd[1]; p->smem_t = sm;
+			p->grid_t = c->nsm * std::min(per, 4);
+			const long n = std::min<long>(ncols, p->grid_t);
+			const long b0 = std::min(((ncols / 3) & ~63L), ncols - n);
+			float ms = -1;
+			for (int rep = 0; rep < 2 && !e; rep++)
+			{
+				e = cudaEventRecord(ev[0], mgcu_stream()) != cudaSuccess ? MG_ERR_DEVICE : 0;
+				if (!e) e = launch_target<P>(p, b0, b0 + n, tmp.as<T>());
+				if (!e) e = cudaEventRecord(ev[1], mgcu_stream()) != cudaSuccess ? MG_ERR_DEVICE : 0;
+				if (!e) e = cudaEventSynchronize(ev[1]) != cudaSuccess ? MG_ERR_DEVICE : 0;
+				if (!e) cudaEventElapsedTime(&ms, ev[0], ev[1]);
+			}
+			if (e) break;
+			if (best_ms < 0 || ms < best_ms) { best_ms = ms; best = cd; }
+		}
+		cudaEventDestroy(ev[0]);
+		cudaEventDestroy(ev[1]);
+		if (e) { mg_set_error("timing the target sweep's block sizes failed"); return e; }
+		t->tuned_sweep[key] = best;
+	}
+	p->threads_t = best[0]; p->nq_t = best[1]; p->smem_t = target_smem_bytes(p, best[0]);
 	return 0;
 }
 
@@ -2522,14 +2620,20 @@ extern "C" mgcu_plan* mgcu_plan_create(const mgcu_plan_desc* d)
 		// threads, one column per block) unless TARGET_DENSE asks for the full one
 		bool wcons = false;
 		if (d->target && d->target->kind == 0 && p->nc_t == 1 && mgcu_option(MG_OPT_TARGET_DENSE_ID) == 0
-			&& (ot <= 0 || tt == 128))
+			&& (ot <= 0 || tt == 128 || tt == 256))
 		{
 			int e = 0, mp = MAXPM, mg = MAXPG;
 			if (p->prec == MG_PREC_FP64_ID) e = target_pm_cap<PrecD>(d->target, p->kt_t, 128, mp, wcons, mg);
 			else if (p->prec == MG_PREC_FP32_ID) e = target_pm_cap<PrecF>(d->target, p->kt_t, 128, mp, wcons, mg);
 			else e = target_pm_cap<PrecX>(d->target, p->kt_t, 128, mp, wcons, mg);
 			if (e) { delete p; return nullptr; }
-			if (wcons) { p->threads_t = tt = 128; p->pm_cap = mp; p->w_t = true; p->maxg_t = mg; }
+			if (wcons)
+			{
+				// 128 threads x two quartets, or 256 x one (TARGET_THREADS 256)
+				p->threads_t = tt = (ot == 256 ? 256 : 128);
+				p->nq_t = tt == 256 ? 1 : 2;
+				p->pm_cap = mp; p->w_t = true; p->maxg_t = mg;
+			}
 		}
 		// room for the staged matrices of the target's busiest pass (built here, cached on the target)
 		if (d->target && d->target->kind == 0 && !p->w_t)
@@ -2541,14 +2645,23 @@ extern "C" mgcu_plan* mgcu_plan_create(const mgcu_plan_desc* d)
 			if (e) { delete p; return nullptr; }
 			p->pm_cap = mp;
 		}
-		p->smem_t = (size_t)p->nc_t * ((size_t)1 << p->kt_t) * p->tsize + 2 * 128 * sizeof(unsigned)
-			+ std::max<size_t>((size_t)(tt / 32) * 16 * sizeof(double), 16 * 16) + (size_t)p->pm_cap * 8 * p->tsize
-			+ (p->w_t ? wtab_bytes(p->kt_t, p->maxg_t) : 0);
+		p->smem_t = target_smem_bytes(p, tt);
+		// the block size by timing (MG_OPT_TARGET_TUNE: 0 = when the trace has at least 2^14
+		// columns, 1 = never, 2 = always) unless TARGET_THREADS fixes it
+		const long tune = mgcu_option(MG_OPT_TARGET_TUNE_ID);
+		if (d->target && d->target->kind == 0 && ot <= 0 && p->nc_t == 1 && tune != 1 && (tune == 2 || d->L >= 14))
+		{
+			int e = 0;
+			if (p->prec == MG_PREC_FP64_ID) e = tune_target_sweep<PrecD>(p);
+			else if (p->prec == MG_PREC_FP32_ID) e = tune_target_sweep<PrecF>(p);
+			else e = tune_target_sweep<PrecX>(p);
+			if (e) { delete p; return nullptr; }
+		}
 	}
 	int per_sm = 1, per_sm_t = 1, e = 0;
-	if (p->prec == MG_PREC_FP64_ID) { e = set_smem_attr<PrecD>(); if (!e) e = occupancy<PrecD>(threads, p->smem, p->kt_t, p->threads_t, p->nc_t, p->smem_t, p->w_t, p->adj, per_sm, per_sm_t); }
-	else if (p->prec == MG_PREC_FP32_ID) { e = set_smem_attr<PrecF>(); if (!e) e = occupancy<PrecF>(threads, p->smem, p->kt_t, p->threads_t, p->nc_t, p->smem_t, p->w_t, p->adj, per_sm, per_sm_t); }
-	else { e = set_smem_attr<PrecX>(); if (!e) e = occupancy<PrecX>(threads, p->smem, p->kt_t, p->threads_t, p->nc_t, p->smem_t, p->w_t, p->adj, per_sm, per_sm_t); }
+	if (p->prec == MG_PREC_FP64_ID) { e = set_smem_attr<PrecD>(); if (!e) e = occupancy<PrecD>(threads, p->smem, p->kt_t, p->threads_t, p->nc_t, p->smem_t, p->w_t, p->nq_t, p->adj, per_sm, per_sm_t); }
+	else if (p->prec == MG_PREC_FP32_ID) { e = set_smem_attr<PrecF>(); if (!e) e = occupancy<PrecF>(threads, p->smem, p->kt_t, p->threads_t, p->nc_t, p->smem_t, p->w_t, p->nq_t, p->adj, per_sm, per_sm_t); }
+	else { e = set_smem_attr<PrecX>(); if (!e) e = occupancy<PrecX>(threads, p->smem, p->kt_t, p->threads_t, p->nc_t, p->smem_t, p->w_t, p->nq_t, p->adj, per_sm, per_sm_t); }
 	if (e) { delete p; return nullptr; }
 	const long opt_cps = mgcu_option(MG_OPT_CTAS_PER_SM_ID);
 	if (opt_cps > 0) per_sm = (int)std::min<long>(per_sm, opt_cps);
@@ -2765,6 +2878,18 @@ extern "C" double mgcu_plan_time_ms(mgcu_plan* p, long b0, long b1, int steps, i
 		total += ms;
 	}
 	return total;
+}
+
+// the target sweep the plan runs: cfg[0] kind (0 none: dense target or host map; 1 full; 2
+// weight-restricted), cfg[1] tile bits, cfg[2] threads, cfg[3] live quartets per thread and
+// iteration (weight-restricted) or columns per block (full)
+extern "C" void mgcu_plan_target_config(const mgcu_plan* p, int* cfg)
+{
+	const bool circ = p->d.target && p->d.target->kind == 0;
+	cfg[0] = circ ? (p->w_t ? 2 : 1) : 0;
+	cfg[1] = p->kt_t;
+	cfg[2] = p->threads_t;
+	cfg[3] = p->w_t ? p->nq_t : p->nc_t;
 }
 
 // k_target launches of the last mgcu_plan_time_ms: their number and summed duration

@@ -759,6 +759,13 @@ int mg_plan_target_kernel_ms(mg_plan* pl, double* ms, long* launches)
 	return e ? MG_ERR_DEVICE : 0;
 }
 
+int mg_plan_target_config(const mg_plan* pl, int cfg[4])
+{
+	if (!pl || !cfg) { mg_set_error("mg_plan_target_config: null argument"); return MG_ERR_ARG; }
+	mgcu_plan_target_config(pl->p, cfg);
+	return 0;
+}
+
 /* ======================================================================================
  * batches
  * ====================================================================================== */

@@ -37,7 +37,8 @@ extern "C" {
 #define MG_OPT_TARGET_DENSE_ID  9
 #define MG_OPT_HOST_THREADS_ID  10
 #define MG_OPT_FIT_CACHE_ID     11
-#define MG_NOPTIONS             11
+#define MG_OPT_TARGET_TUNE_ID   12
+#define MG_NOPTIONS             12
 
 /* ---- runtime ---- */
 /* streams: each host thread issues its GPU work on its own stream when it selected one
@@ -137,6 +138,7 @@ int mgcu_batch_project(mgcu_batch* b, int i, const mgg* vblocks, double* grad_ve
 int mgcu_batch_info(const mgcu_batch* b, int i, int* target_tile_bits, int* target_passes, int* items);
 double mgcu_batch_time_ms(mgcu_batch* b, int steps, int flush_l2);
 int mgcu_plan_target_kernel_ms(mgcu_plan* p, double* ms, long* launches);
+void mgcu_plan_target_config(const mgcu_plan* p, int* cfg);
 
 /* ---- FP64 algebra on the GPU ---- */
 int mgcu_retract(const mgg* u, const double* eta, int n, mgg* v);

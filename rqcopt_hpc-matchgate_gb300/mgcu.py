@@ -27,6 +27,7 @@ OPT_TRANSLATIONAL_INVARIANCE = 8
 OPT_TARGET_DENSE = 9
 OPT_HOST_THREADS = 10
 OPT_FIT_CACHE = 11
+OPT_TARGET_TUNE = 12
 EVAL_TARGET, EVAL_GRADIENT, EVAL_HESSIAN, EVAL_TI = 0, 1, 2, 4
 
 P = C.c_void_p
@@ -154,6 +155,7 @@ class MatchgateLib:
             L.mg_plan_time_ms.argtypes = [P, C.c_int, C.c_int]
             L.mg_plan_time_ms.restype = C.c_double
             L.mg_plan_target_kernel_ms.argtypes = [P, P, P]
+            L.mg_plan_target_config.argtypes = [P, P]
             L.mg_launch_count.restype = C.c_long
             L.mg_get_option.restype = C.c_long
             L.mg_set_option.argtypes = [C.c_int, C.c_long]
@@ -176,6 +178,15 @@ class MatchgateLib:
 
     def last_error(self):
         return self.lib.mg_last_error().decode()
+
+    def plan_target_config(self, plan):
+        """the plan's target sweep: dict(kind 0 none / 1 full / 2 weight-restricted, tile_bits,
+        threads, per_thread)"""
+        cfg = (C.c_int * 4)()
+        rc = self.lib.mg_plan_target_config(P(plan), cfg)
+        if rc != 0:
+            raise RuntimeError(self.last_error())
+        return {"kind": cfg[0], "tile_bits": cfg[1], "threads": cfg[2], "per_thread": cfg[3]}
 
     def plan_target_kernel_ms(self, plan):
         """(summed ms, launches) of the target-sweep kernel in the last plan timing"""
