@@ -129,6 +129,17 @@ int mg_optimize_circuit(void* target, const struct matchgate gates0[], int ngate
 int mg_hubbard_trotter_circuit(int nsites, double J, double U, double t, int nsteps, int order,
                                struct matchgate gates[], int wires[], int capacity);
 void* mg_target_hubbard(int nsites, double J, double U, double t, int nsteps, int order);
+/* The spinless chain of the reference's published benchmark: L sites on a ring (periodic
+ * wiring), h = -J (|01><10| + |10><01|) + g |11><11| per bond, even and odd bonds as the two
+ * terms, as a brickwall with one matchgate per layer (exp(-i tau h) on all L/2 pairs of the
+ * layer's permutation: identity for even bonds, shifted by one for odd bonds), neighbouring
+ * layers of one term merged.  mg_spinless_hubbard_brickwall writes ulist[n] and the
+ * permutations perms[n * L] (row l = layer l) when capacity >= n and returns the layer count
+ * n (< 0 on bad arguments); mg_target_spinless_hubbard returns a GPU target of it (12 steps
+ * of order 6 at L=16 give the 601-layer target of the published runs). */
+int mg_spinless_hubbard_brickwall(int L, double J, double g, double t, int nsteps, int order,
+                                  struct matchgate ulist[], int perms[], int capacity);
+void* mg_target_spinless_hubbard(int L, double J, double g, double t, int nsteps, int order);
 
 /* ---------------------------------------------------------------------------------
  * Batches: f and the layer gradients of many independent brickwall fits at once, each

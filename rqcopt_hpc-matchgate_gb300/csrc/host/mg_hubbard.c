@@ -44,19 +44,19 @@ static int rule_push(rule_t* r, int term, double c)
 	return 0;
 }
 
-/* the layers of S_2k(scale) appended to r */
-static int suzuki(rule_t* r, int k, double scale)
+/* the layers of S_2k(scale) over nterms terms appended to r: S_2 = the terms forward then
+ * backward, each with coefficient 1/2 (the middle term's two halves merge) */
+static int suzuki(rule_t* r, int k, double scale, int nterms)
 {
 	if (k == 1)
 	{
-		static const int seq[5] = { 0, 1, 2, 1, 0 };
-		static const double cf[5] = { 0.5, 0.5, 1.0, 0.5, 0.5 };
-		for (int i = 0; i < 5; i++) if (rule_push(r, seq[i], cf[i] * scale)) return -1;
+		for (int i = 0; i < nterms; i++) if (rule_push(r, i, 0.5 * scale)) return -1;
+		for (int i = nterms - 1; i >= 0; i--) if (rule_push(r, i, 0.5 * scale)) return -1;
 		return 0;
 	}
 	const double p = 1.0 / (4.0 - pow(4.0, 1.0 / (2 * k - 1)));
 	const double w[5] = { p, p, 1 - 4 * p, p, p };
-	for (int i = 0; i < 5; i++) if (suzuki(r, k - 1, w[i] * scale)) return -1;
+	for (int i = 0; i < 5; i++) if (suzuki(r, k - 1, w[i] * scale, nterms)) return -1;
 	return 0;
 }
 
@@ -114,7 +114,7 @@ static int hubbard_build(int nsites, double J, double U, double t, int nsteps, i
 	rule_t r = { 0 };
 	const double h = t / nsteps;
 	for (int s = 0; s < nsteps; s++)
-		if (suzuki(&r, order / 2, h)) { free(r.term); free(r.coeff); return -1; }
+		if (suzuki(&r, order / 2, h, 3)) { free(r.term); free(r.coeff); return -1; }
 	const struct matchgate fswap = mk(0, 1, 1, 0, 1, 0, 0, -1);
 	int rc = 0;
 	for (int l = 0; l < r.n && !rc; l++)
@@ -163,5 +163,63 @@ void* mg_target_hubbard(int nsites, double J, double U, double t, int nsteps, in
 	if (hubbard_build(nsites, J, U, t, nsteps, order, &s)) { free(s.g); free(s.w); return NULL; }
 	void* h = mg_target_circuit(s.g, s.n, s.w, 2 * nsites);
 	free(s.g); free(s.w);
+	return h;
+}
+
+/*
+ * The spinless 1-D Fermi-Hubbard brickwall of the reference's published benchmark
+ * (benchmark_hpc/spl_hubbard1d_bench_init.py:24-118): L sites on a ring, Jordan-Wigner
+ * encoded, H = sum over bonds of h = -J (|01><10| + |10><01|) + g |11><11|; terms = the even
+ * bonds (pairs (0,1), (2,3), ...) and the odd bonds ((1,2), ..., (L-1,0)); nsteps steps of
+ * Suzuki's order-`order` rule over time t, neighbouring layers of one term merged.  Each
+ * layer is one matchgate exp(-i tau h) (center exp(i tau J X), corner diag(1, e^{-i tau g}))
+ * on all L/2 pairs of its permutation.  Writes the layers when capacity suffices and returns
+ * their count (< 0 on bad arguments).
+ */
+static int spinless_build(int L, double J, double g, double t, int nsteps, int order, rule_t* r)
+{
+	if (L < 4 || L > 30 || L % 2 || nsteps < 1 || order < 2 || order % 2 || order > 12)
+	{
+		mg_set_error("spinless Hubbard brickwall: need an even 4 <= L <= 30, nsteps >= 1 and an even order 2..12");
+		return MG_ERR_ARG;
+	}
+	const double h = t / nsteps;
+	for (int s = 0; s < nsteps; s++)
+		if (suzuki(r, order / 2, h, 2)) return -1;
+	return 0;
+}
+
+int mg_spinless_hubbard_brickwall(int L, double J, double g, double t, int nsteps, int order,
+	struct matchgate ulist[], int perms[], int capacity)
+{
+	rule_t r = { 0 };
+	int rc = spinless_build(L, J, g, t, nsteps, order, &r);
+	if (!rc && ulist && perms && capacity >= r.n)
+		for (int l = 0; l < r.n; l++)
+		{
+			const double tau = r.coeff[l], c = cos(J * tau), sn = sin(J * tau);
+			ulist[l] = mk(c, I * sn, I * sn, c, 1, 0, 0, cexp(-I * g * tau));
+			for (int q = 0; q < L; q++) perms[l * L + q] = r.term[l] == 0 ? q : (q + 1) % L;
+		}
+	if (!rc) rc = r.n;
+	free(r.term); free(r.coeff);
+	return rc;
+}
+
+void* mg_target_spinless_hubbard(int L, double J, double g, double t, int nsteps, int order)
+{
+	const int n = mg_spinless_hubbard_brickwall(L, J, g, t, nsteps, order, NULL, NULL, 0);
+	if (n < 0) return NULL;
+	struct matchgate* u = malloc(sizeof(struct matchgate) * n);
+	int* pm = malloc(sizeof(int) * (size_t)n * L);
+	const int** rows = malloc(sizeof(int*) * n);
+	void* h = NULL;
+	if (u && pm && rows && mg_spinless_hubbard_brickwall(L, J, g, t, nsteps, order, u, pm, n) == n)
+	{
+		for (int l = 0; l < n; l++) rows[l] = pm + (size_t)l * L;
+		h = mg_target_brickwall(u, n, rows, L);
+	}
+	else if (!(u && pm && rows)) mg_set_error("spinless Hubbard brickwall: out of host memory");
+	free(u); free(pm); free(rows);
 	return h;
 }

@@ -136,6 +136,9 @@ class MatchgateLib:
             L.mg_hubbard_trotter_circuit.argtypes = [C.c_int, C.c_double, C.c_double, C.c_double, C.c_int, C.c_int, P, P, C.c_int]
             L.mg_target_hubbard.restype = P
             L.mg_target_hubbard.argtypes = [C.c_int, C.c_double, C.c_double, C.c_double, C.c_int, C.c_int]
+            L.mg_spinless_hubbard_brickwall.argtypes = [C.c_int, C.c_double, C.c_double, C.c_double, C.c_int, C.c_int, P, P, C.c_int]
+            L.mg_target_spinless_hubbard.restype = P
+            L.mg_target_spinless_hubbard.argtypes = [C.c_int, C.c_double, C.c_double, C.c_double, C.c_int, C.c_int]
             L.mg_optimize_brickwall.argtypes = [P, P, C.c_int, C.c_int, P, C.POINTER(RtrParams), C.c_int, C.c_double, P, P, P]
             L.mg_server_create.restype = P
             L.mg_server_create.argtypes = [C.c_size_t, C.c_int]
@@ -287,6 +290,16 @@ class MatchgateLib:
         n2 = self.lib.mg_hubbard_trotter_circuit(nsites, J, U, t, nsteps, order, _p(g), _p(w), n)
         assert n2 == n
         return g, w
+
+    def spinless_hubbard_brickwall(self, L, J, g, t, nsteps, order=2):
+        """(ulist [n, 8], perms [n, L]) of the spinless brickwall built by the library"""
+        n = self.lib.mg_spinless_hubbard_brickwall(L, J, g, t, nsteps, order, None, None, 0)
+        if n < 0:
+            raise RuntimeError(self.last_error())
+        u = np.zeros((n, 8), cd); pm = np.zeros((n, L), np.int32)
+        n2 = self.lib.mg_spinless_hubbard_brickwall(L, J, g, t, nsteps, order, _p(u), _p(pm), n)
+        assert n2 == n
+        return u, pm
 
     # ------------------------------------------------------------------ request server
     def server_create(self, budget_bytes, max_batch=256):

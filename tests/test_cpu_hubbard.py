@@ -86,3 +86,23 @@ def test_spinless_hubbard_brickwall_matches_generator_conventions():
     i6, c6 = T.suzuki_rule(2, 3)
     assert len(i6) == 51
     assert abs(sum(c for i, c in zip(i6, c6) if i == 0) - 1) < 1e-13 and abs(sum(c for i, c in zip(i6, c6) if i == 1) - 1) < 1e-13
+
+
+@pytest.mark.parametrize("L,nsteps,order", [(16, 12, 6), (16, 2, 2), (8, 3, 4), (6, 1, 2)])
+def test_spinless_brickwall_matches_python_construction(mglib, L, nsteps, order):
+    """the library's spinless brickwall (the published benchmark's target: L=16, 12 steps of
+    order 6 = 601 layers; its fit: 2 steps of order 2 = 5 layers) equals targets.py's layer by
+    layer"""
+    u, pm = mglib.spinless_hubbard_brickwall(L, 1.0, 1.5, 1.0, nsteps, order)
+    u2, pm2 = T.spinless_hubbard_brickwall(L, 1.0, 1.5, 1.0, nsteps, order)
+    assert u.shape == u2.shape and np.array_equal(pm, pm2)
+    assert np.max(np.abs(u - u2)) < 1e-14
+    if (L, nsteps, order) == (16, 12, 6):
+        assert len(u) == 601
+    if (L, nsteps, order) == (16, 2, 2):
+        assert len(u) == 5
+
+
+def test_spinless_brickwall_bad_arguments(mglib):
+    for args in [(5, 1.0, 1.5, 1.0, 2, 2), (16, 1.0, 1.5, 1.0, 0, 2), (16, 1.0, 1.5, 1.0, 2, 3)]:
+        assert mglib.lib.mg_spinless_hubbard_brickwall(*args, None, None, 0) < 0
