@@ -56,11 +56,16 @@ int mg_get_precision(void);
  * TARGET_THREADS is 0.  0 (default): by timing the candidates (128 or 256 threads, and for
  * the full sweep 512) on one resident wave of columns when the trace has at least 2^14
  * columns, once per target, precision and tile size; 1: never (128 threads); 2: always.
- * The candidates give bit-identical results. */
+ * The candidates give bit-identical results.
+ * HESS_GROUP: how a plain Hessian of parameter blocks shared by several gates (the per-layer
+ * brickwall Hessian) is computed.  0 (default): one forward-mode sweep per basis column,
+ * block and entry, which adds each of the block's gates' placeholder terms as it passes them
+ * (a sixth of the gate steps at L=16 with 5 layers); 1: one sweep per gate and entry, the
+ * reference's placements (src/matchgate_brickwall.c:177-231).  The two agree to rounding. */
 enum { MG_OPT_TILE_BITS = 1, MG_OPT_THREADS = 2, MG_OPT_CHUNK_COLUMNS = 3, MG_OPT_CTAS_PER_SM = 4,
        MG_OPT_TARGET_TILE_BITS = 5, MG_OPT_TARGET_THREADS = 6, MG_OPT_TARGET_COLUMNS = 7,
        MG_OPT_TRANSLATIONAL_INVARIANCE = 8, MG_OPT_TARGET_DENSE = 9, MG_OPT_HOST_THREADS = 10,
-       MG_OPT_FIT_CACHE = 11, MG_OPT_TARGET_TUNE = 12 };
+       MG_OPT_FIT_CACHE = 11, MG_OPT_TARGET_TUNE = 12, MG_OPT_HESS_GROUP = 13 };
 int mg_set_option(int option, long value);
 long mg_get_option(int option);
 

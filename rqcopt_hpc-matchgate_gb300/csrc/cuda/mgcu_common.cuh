@@ -123,6 +123,7 @@ struct PrecD
 	}
 	__device__ static T negconj(T a) { return make_double2(-a.x, a.y); }
 	__device__ static T neg(T a) { return make_double2(-a.x, -a.y); }
+	__device__ static T add(T a, T b) { return make_double2(a.x + b.x, a.y + b.y); }
 	// a with its sign flipped when s == 1 (bit operations, no arithmetic)
 	__device__ static T negif(T a, unsigned s)
 	{
@@ -183,6 +184,7 @@ struct PrecF
 	}
 	__device__ static T negconj(T a) { return make_float2(-a.x, a.y); }
 	__device__ static T neg(T a) { return make_float2(-a.x, -a.y); }
+	__device__ static T add(T a, T b) { return make_float2(a.x + b.x, a.y + b.y); }
 	__device__ static T negif(T a, unsigned s)
 	{
 		const unsigned m = s << 31;
@@ -258,6 +260,14 @@ struct PrecX
 	}
 	__device__ static T negconj(T a) { return make_float4(-a.x, a.y, -a.z, a.w); }
 	__device__ static T neg(T a) { return make_float4(-a.x, -a.y, -a.z, -a.w); }
+	// a + b: hi = the rounded sum of the hi parts, lo = its exact error plus both lo parts
+	__device__ static T add(T a, T b)
+	{
+		float rh, re, ih, ie;
+		two_sum(a.x, b.x, rh, re);
+		two_sum(a.y, b.y, ih, ie);
+		return make_float4(rh, ih, __fadd_rn(re, __fadd_rn(a.z, b.z)), __fadd_rn(ie, __fadd_rn(a.w, b.w)));
+	}
 	__device__ static T negif(T a, unsigned s)
 	{
 		const unsigned m = s << 31;

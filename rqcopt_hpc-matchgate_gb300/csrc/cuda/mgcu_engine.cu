@@ -281,6 +281,7 @@ struct Args
 	const int* pass_of;
 	const int* block;          // [ngates]
 	int nplace, mdim;          // mdim = 8 * nblocks
+	int hgroup;                // 1: a placement is its gate's whole block (every gate of the block adds its placeholder term)
 	double* part_h;            // [grid][mdim][mdim][2]
 	T* sh;                     // per-block slot for placeholder states
 	T* ucols;                  // k_target: output columns [b - b0][S]
@@ -1567,6 +1568,17 @@ __global__ void __launch_bounds__(256, 2) k_batch(const Args<P>* __restrict__ ar
 // derivative (reference src/matchgate_brickwall.c:177-231).  Consecutive gates of a
 // pass with the same block and weight (a brickwall layer) share one block reduction:
 // the thread accumulators carry over, up to HESS_MERGE quartets per thread.
+//
+// Grouped placements (hgroup, the plain Hessian of parameter blocks shared by several
+// gates, as the reference's per-layer brickwall Hessian): an item is (column, block,
+// entry) and carries the derivative of the state with respect to that entry of the
+// block's matrix, forward mode: it starts as the placeholder state at the block's first
+// gate, and at every later gate s of the block, B <- G_s B + placeholder_s(input of s).
+// Contracting B with the cached derivative at a gate s gives the sum over the block's
+// gates r < s of what the per-gate items (r, entry) contribute there, so one item does
+// the work of all the block's placements: at L=16 with 5 layers, 120 instead of 780
+// gate steps per column and entry.  The same pairs (r < s) land in the same Hessian
+// blocks, so the symmetrisation that follows is unchanged.
 // ------------------------------------------------------------------------------------
 constexpr int HESS_MERGE = 64;
 
@@ -1602,6 +1614,7 @@ __global__ void __launch_bounds__(256, 2) k_hessian(Args<P> a, long nitems)
 		const T* dcache = a.dcache + (size_t)bi * a.ngates * S;
 		const double* wrow = a.place_w + (size_t)p * a.ngates;
 		double* hrow = parth + (size_t)(a.block[k] * 8 + x) * a.mdim * 2;
+		const int grp = a.hgroup ? a.block[k] : -1;
 		for (int pp = pk; pp < a.W.npass; pp++)
 		{
 			const PassRec& pr = a.W.pass[pp];
@@ -1654,6 +1667,9 @@ __global__ void __launch_bounds__(256, 2) k_hessian(Args<P> a, long nitems)
 					const Gate8<T> G = load_gate(a.wm, r.g);
 					const T* dg = dcache + (size_t)r.g * S + ((size_t)tau << kt);   // tile order
 					const bool apply = (r.g != a.ngates - 1);
+					// grouped placement: this gate of the block adds its placeholder term
+					// (entry x of its input, cached in tile order) after the gate
+					const T* cg = (grp >= 0 && a.block[r.g] == grp) ? cache + (size_t)r.g * S + ((size_t)tau << kt) : nullptr;
 					const int blk = a.block[r.g];
 					const double wg = wrow[r.g];
 					// the next gate of the pass (a later one: passes keep the sequential
@@ -1673,10 +1689,20 @@ __global__ void __launch_bounds__(256, 2) k_hessian(Args<P> a, long nitems)
 						contract_quartet<P>(acc, dg[ex], dg[ew], dg[ey], dg[ez], vx, vw, vy, vz);
 						if (apply)
 						{
-							tile[ex] = P::madd2(G.k0, vx, G.k1, vw);
-							tile[ew] = P::madd2(G.k2, vx, G.k3, vw);
-							tile[ey] = P::madd2(G.c0, vy, G.c1, vz);
-							tile[ez] = P::madd2(G.c2, vy, G.c3, vz);
+							T ox = P::madd2(G.k0, vx, G.k1, vw), ow = P::madd2(G.k2, vx, G.k3, vw);
+							T oy = P::madd2(G.c0, vy, G.c1, vz), oz = P::madd2(G.c2, vy, G.c3, vz);
+							if (cg)
+							{
+								// entry x of the block: output (x >> 1) & 1 of the center (x < 4) or
+								// corner block gains input x & 1 of the same block
+								const unsigned ein = x < 4 ? ((x & 1) ? ez : ey) : ((x & 1) ? ew : ex);
+								const T c = cg[ein];
+								if (x < 2) oy = P::add(oy, c);
+								else if (x < 4) oz = P::add(oz, c);
+								else if (x < 6) ox = P::add(ox, c);
+								else ow = P::add(ow, c);
+							}
+							tile[ex] = ox; tile[ew] = ow; tile[ey] = oy; tile[ez] = oz;
 						}
 					}
 					if (flush)
@@ -2322,6 +2348,7 @@ struct mgcu_plan
 	Sched ws;
 	DevBuf d_pass, d_gate, d_mats, d_pass_of, d_block, d_place, d_placew;
 	bool adj = false;              // gradient plan: checkpointed backward sweep (k_columns_adj)
+	bool hgroup = false;           // Hessian plan: one item per (column, block, entry), see k_hessian
 	bool adj_ok = false;           // the current gates are invertible (else the cached sweep)
 	DevBuf d_mats_inv, ck;
 	DevBuf su, sw, sh, cache, dcache, part_f, part_g, part_h, cols64, cols;
@@ -2425,7 +2452,7 @@ static int launch_columns(mgcu_plan* p, long b0, long b1, const typename P::T* d
 	if (p->d.want_hess)
 	{
 		a.place = p->d_place.as<int>(); a.place_w = p->d_placew.as<double>(); a.pass_of = p->d_pass_of.as<int>();
-		a.block = p->d_block.as<int>(); a.nplace = p->d.nplace; a.mdim = 8 * p->d.nblocks;
+		a.block = p->d_block.as<int>(); a.nplace = p->d.nplace; a.mdim = 8 * p->d.nblocks; a.hgroup = p->hgroup ? 1 : 0;
 		a.part_h = p->part_h.as<double>(); a.sh = p->sh.as<T>();
 		const long nitems = ncols * p->d.nplace * 8;
 		const int gb = (int)std::min<long>(p->grid_b, nitems);
@@ -2564,6 +2591,30 @@ extern "C" mgcu_plan* mgcu_plan_create(const mgcu_plan_desc* d)
 	{
 		p->place.assign(d->place, d->place + d->nplace);
 		p->place_w.assign(d->place_w, d->place_w + (size_t)d->nplace * d->ngates);
+		// the plain placements (every gate, unit weights on every later gate) of parameter
+		// blocks shared by several gates become one grouped placement per block, at the
+		// block's first gate (k_hessian's forward-mode items)
+		const int ng = d->ngates;
+		bool plain = d->nplace == ng && d->nblocks < ng && d->place && d->place_w && mgcu_option(MG_OPT_HESS_GROUP_ID) != 1;
+		for (int q = 0; q < ng && plain; q++)
+		{
+			plain = d->place[q] == q;
+			for (int l = 0; l < ng && plain; l++) plain = d->place_w[(size_t)q * ng + l] == (l > q ? 1.0 : 0.0);
+		}
+		if (plain)
+		{
+			std::vector<int> first(d->nblocks, -1);
+			for (int g = 0; g < ng; g++)
+				if (p->block[g] >= 0 && p->block[g] < d->nblocks && first[p->block[g]] < 0) first[p->block[g]] = g;
+			p->place.clear();
+			for (int b = 0; b < d->nblocks; b++) if (first[b] >= 0) p->place.push_back(first[b]);
+			std::sort(p->place.begin(), p->place.end());
+			p->place_w.assign(p->place.size() * (size_t)ng, 0.0);
+			for (size_t q = 0; q < p->place.size(); q++)
+				for (int l = p->place[q] + 1; l < ng; l++) p->place_w[q * ng + l] = 1.0;
+			p->d.nplace = (int)p->place.size();
+			p->hgroup = true;
+		}
 	}
 	p->d.wires = p->wires.data(); p->d.block = p->block.data();
 	p->d.place = p->place.data(); p->d.place_w = p->place_w.data();
@@ -2710,15 +2761,15 @@ extern "C" mgcu_plan* mgcu_plan_create(const mgcu_plan_desc* d)
 	if (!e) e = p->d_pass_of.alloc(sizeof(int) * ng);
 	if (!e) e = p->cols.alloc(col_bytes * chunk);
 	if (!e && !d->target) e = p->cols64.alloc((size_t)p->S * 16 * chunk);
-	if (!e && d->want_hess) e = p->d_place.alloc(sizeof(int) * std::max(d->nplace, 1));
-	if (!e && d->want_hess) e = p->d_placew.alloc(sizeof(double) * std::max<size_t>((size_t)d->nplace * ng, 1));
+	if (!e && d->want_hess) e = p->d_place.alloc(sizeof(int) * std::max(p->d.nplace, 1));
+	if (!e && d->want_hess) e = p->d_placew.alloc(sizeof(double) * std::max<size_t>((size_t)p->d.nplace * ng, 1));
 	if (e) { delete p; return nullptr; }
 	cudaStream_t st = mgcu_stream();
 	bool ok = cudaMemcpyAsync(p->d_block.p, p->block.data(), sizeof(int) * ng, cudaMemcpyHostToDevice, st) == cudaSuccess;
 	ok = ok && cudaMemcpyAsync(p->d_pass_of.p, p->ws.pass_of.data(), sizeof(int) * d->ngates, cudaMemcpyHostToDevice, st) == cudaSuccess;
 	if (d->want_hess)
 	{
-		ok = ok && cudaMemcpyAsync(p->d_place.p, p->place.data(), sizeof(int) * d->nplace, cudaMemcpyHostToDevice, st) == cudaSuccess;
+		ok = ok && cudaMemcpyAsync(p->d_place.p, p->place.data(), sizeof(int) * p->d.nplace, cudaMemcpyHostToDevice, st) == cudaSuccess;
 		ok = ok && cudaMemcpyAsync(p->d_placew.p, p->place_w.data(), sizeof(double) * p->place_w.size(), cudaMemcpyHostToDevice, st) == cudaSuccess;
 	}
 	ok = ok && cudaStreamSynchronize(st) == cudaSuccess;

@@ -38,7 +38,8 @@ extern "C" {
 #define MG_OPT_HOST_THREADS_ID  10
 #define MG_OPT_FIT_CACHE_ID     11
 #define MG_OPT_TARGET_TUNE_ID   12
-#define MG_NOPTIONS             12
+#define MG_OPT_HESS_GROUP_ID    13
+#define MG_NOPTIONS             13
 
 /* ---- runtime ---- */
 /* streams: each host thread issues its GPU work on its own stream when it selected one
