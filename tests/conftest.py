@@ -71,6 +71,20 @@ def helpers():
 
 
 @pytest.fixture(scope="session")
+def trdriver(mglib):
+    """tests/helpers/mg_test_tr_driver.c built against include/ and linked to libmgcu.so
+    (fails, not skips, when it cannot be built)"""
+    out_dir = os.path.join(ROOT, "tests", "_build")
+    os.makedirs(out_dir, exist_ok=True)
+    src = os.path.join(ROOT, "tests", "helpers", "mg_test_tr_driver.c")
+    so = os.path.join(out_dir, "libmgtrdriver.so")
+    libdir = os.path.dirname(mglib.path)
+    subprocess.run(["gcc", "-O2", "-std=gnu11", "-fPIC", "-shared", "-DCOMPLEX_CIRCUIT", "-I", os.path.join(ROOT, "include"),
+                    "-o", so, src, "-L", libdir, "-lmgcu", "-Wl,-rpath," + libdir, "-Wl,--no-undefined"], check=True)
+    return ctypes.CDLL(so)
+
+
+@pytest.fixture(scope="session")
 def mglib():
     import importlib.util
     spec = importlib.util.spec_from_file_location("mg_pkg_build", os.path.join(PKG, "build.py"))

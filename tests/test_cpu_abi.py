@@ -102,3 +102,9 @@ def test_reference_optimiser_links(mglib, tmp_path):
     r = subprocess.run(["gcc", "-std=gnu11", "-DCOMPLEX_CIRCUIT", "-I", INCLUDE, "-I", str(tmp_path), str(main), str(obj), "-L", libdir, "-lmgcu",
                         "-Wl,-rpath," + libdir, "-Wl,--no-undefined", "-o", str(exe)], capture_output=True, text=True)
     assert r.returncode == 0, r.stderr
+
+
+def test_c_driver_builds_against_the_headers(trdriver):
+    """tests/helpers/mg_test_tr_driver.c (a C caller with the reference's optimiser glue)
+    compiles against include/ and links to libmgcu.so with every symbol resolved"""
+    assert hasattr(trdriver, "mgt_optimize_brickwall_hmat")

@@ -98,6 +98,39 @@ def test_trust_region_matches_oracle(lib, oracle):
     assert f_g[-1] < f_g[0]
 
 
+def test_c_driver_trust_region_matches_oracle(lib, oracle, trdriver):
+    """the same 10 iterations driven from C (tests/helpers/mg_test_tr_driver.c: the
+    reference's optimiser glue, src/mg_brickwall_opt.c:99-122, compiled against include/ and
+    linked to libmgcu.so): f_iter, f_citer and the final gates equal the oracle's"""
+    import ctypes as C
+    rng = np.random.default_rng(1)
+    L, nl, ul = 8, 4, 8
+    perms = brickwall_perms(L, nl)
+    uperms = brickwall_perms(L, ul)
+    ulist = random_gates(ul, rng, unitary=True)
+    v0 = np.ascontiguousarray(random_gates(nl, rng, unitary=True), np.complex128)
+    niter = 10
+    lib.set_precision(mgcu.PREC_FP64)
+    t = lib.target_brickwall(ulist, uperms, L)
+    pr = np.ascontiguousarray(np.asarray(perms, np.int32).reshape(nl, L))
+    rows = (C.c_void_p * nl)(*[pr[i].ctypes.data for i in range(nl)])
+    f_iter = np.zeros(niter + 1)
+    f_citer = np.zeros(niter + 1, np.complex128)
+    vopt = np.zeros((nl, 8), np.complex128)
+    try:
+        rc = trdriver.mgt_optimize_brickwall_hmat(C.c_void_p(lib.mg_target_apply), C.c_void_p(t),
+                                                  C.c_void_p(v0.ctypes.data), nl, L, rows, niter, C.c_void_p(f_iter.ctypes.data),
+                                                  C.c_void_p(f_citer.ctypes.data), C.c_void_p(vopt.ctypes.data))
+    finally:
+        lib.target_free(t)
+    assert rc == 0
+    f_o, fc_o, v_o = oracle.rtr_brickwall(oracle.Target("brickwall", L, ulist=ulist, uperms=uperms), v0, perms, L, niter)
+    assert np.max(np.abs(f_iter - f_o)) < 1e-8
+    assert np.max(np.abs(f_citer - fc_o)) < 1e-8
+    assert udist(vopt, v_o) < 1e-8
+    assert f_iter[-1] < f_iter[0]
+
+
 def test_native_trust_region_and_refinement(lib, oracle):
     """mg_optimize_brickwall: complex128 throughout matches the oracle's 10 iterations;
     float-float first with the switch to complex128 near convergence reaches the same
