@@ -9,7 +9,9 @@
  * (src/matchgate_target.c:877-973), Steihaug tCG, retraction per layer, the rho test
  * (rho < 1/4 shrinks the radius by 4, rho > 3/4 on the boundary doubles it up to maxradius,
  * the step is taken when rho > rho_trust).  mg_optimize_circuit runs the same loop on a
- * general circuit with one parameter block per gate.
+ * general circuit with one parameter block per gate.  The last f_iter entry, f at the final
+ * iterate, reuses the evaluation of the accepted trial point that became that iterate (the
+ * reference evaluates the same point once more; the value is the same, bit for bit).
  */
 #include <complex.h>
 #include <math.h>
@@ -97,6 +99,11 @@ static int optimize(void* target, const struct matchgate vlist0[], const fit_t* 
 	int prec = refine_gnorm > 0 ? MG_PREC_MIXED : MG_PREC_FP64;
 	int rc = plans_make(&pl, target, x, fit, prec);
 	double radius = params->radius_init;
+	/* f of the current iterate from a target-only evaluation at the current precision, when
+	 * one was made (the trial point of an accepted step): the final f_iter entry reuses it
+	 * instead of evaluating the same point again, with the same plan and the same bits */
+	double fcur = 0;
+	int fcur_ok = 0;
 	for (int k = 0; k < niter && !rc; k++)
 	{
 		double fx;
@@ -110,6 +117,7 @@ static int optimize(void* target, const struct matchgate vlist0[], const fit_t* 
 			{
 				/* near convergence: complex128 from here on, this iterate re-evaluated */
 				prec = MG_PREC_FP64;
+				fcur_ok = 0;
 				rc = plans_make(&pl, target, x, fit, prec);
 				if (!rc) rc = eval_hess(&pl, x, &fx, grad, H);
 				if (rc) break;
@@ -133,11 +141,17 @@ static int optimize(void* target, const struct matchgate vlist0[], const fit_t* 
 		const double rho = (fn - fx) / (ge + 0.5 * eHe);
 		if (rho < 0.25) radius *= 0.25;
 		else if (rho > 0.75 && on_boundary) radius = fmin(2 * radius, params->maxradius);
-		if (rho > params->rho_trust) memcpy(x, xn, sizeof(struct matchgate) * nlayers);
+		if (rho > params->rho_trust)
+		{
+			memcpy(x, xn, sizeof(struct matchgate) * nlayers);
+			fcur = fn;
+			fcur_ok = 1;
+		}
 	}
 	if (!rc)
 	{
-		rc = eval_f(&pl, x, &f_iter[niter]);
+		if (fcur_ok) f_iter[niter] = fcur;
+		else rc = eval_f(&pl, x, &f_iter[niter]);
 		if (prec_iter) prec_iter[niter] = prec;
 		memcpy(vlist_out, x, sizeof(struct matchgate) * nlayers);
 	}
