@@ -57,7 +57,10 @@ def parse():
                          "benchmark (L=16, 5 layers, 601-layer target); hostmap: L=14 with the target as a host map")
     ap.add_argument("--published-hessian", default="both", choices=["plain", "ti", "both"])
     ap.add_argument("--published-precision", default="both", choices=["mixed", "fp64", "both"])
-    ap.add_argument("--resident", action="store_true", help="--config published: keep the target columns on the GPU")
+    ap.add_argument("--resident", action="store_true", help="--config published: make the target resident before the fit")
+    ap.add_argument("--published-sweep", action="store_true",
+                    help="--config published: sweep the target in every evaluation (MG_OPT_FIT_RESIDENT 1), as the "
+                         "reference applies its target map each time")
     ap.add_argument("--serve-requests", type=int, default=60,
                     help="--config serve: the first this many requests of the seeded stream (a time-bounded prefix)")
     ap.add_argument("--serve-hess-max-L", type=int, default=12, help="largest L of Hessian and trust-region-step requests")
@@ -550,13 +553,15 @@ def run_published(a):
     niter = 1 and set_rtr_default_params(16 nlayers), i.e. f + Riemannian gradient + Hessian,
     tCG, retraction, f at the trial point, f at the final point; src/trust_region.c:235-306),
     on this library's native trust-region driver, plain and translation-invariant Hessian, in
-    float-float and in complex128; wall time of the synchronous call.  With --resident the
-    target's columns stay on the GPU after the first evaluation (the target is fixed within
-    a fit), which the reference does not do."""
+    float-float and in complex128; wall time of the synchronous call.  By default the native
+    fit keeps the target's columns on the GPU after the first evaluation (the target is fixed
+    within a fit; MG_OPT_FIT_RESIDENT 0), which the reference does not do; --published-sweep
+    sweeps the target in every evaluation as the reference does."""
     import numpy as np
     import mgcu
     lib = mgcu.default_lib()
     L = 16
+    lib.set_option(mgcu.OPT_FIT_RESIDENT, 1 if a.published_sweep else 0)
     ul, up, v, perms = published_workload(L)
     target = lib.target_brickwall(ul, up, L)
     rows = {}
@@ -575,6 +580,7 @@ def run_published(a):
                                     "speedup_vs_published": PUBLISHED_S[h] / dt,
                                     "f_iter": [float(x) for x in f_iter], "gates_out": vout}
     lib.set_option(mgcu.OPT_TRANSLATIONAL_INVARIANCE, 0)
+    lib.set_option(mgcu.OPT_FIT_RESIDENT, 0)
     lib.target_free(target)
     acc = {}
     for h in hess:
@@ -594,7 +600,10 @@ def run_published(a):
                 "steps target, order 2 x 2 steps fit)",
         "config": {"workload": "optimize_matchgate_brickwall_circuit_hmat, niter=1: f + Riemannian gradient + Hessian, tCG "
                                "(maxiter 160), retraction, 2 f", "L": L, "nlayers": len(v), "target_layers": len(ul),
-                   "target_gates": len(ul) * (L // 2), "resident_target": bool(a.resident)},
+                   "target_gates": len(ul) * (L // 2),
+                   "target_columns": ("swept in every evaluation (MG_OPT_FIT_RESIDENT 1)" if a.published_sweep else
+                                      "kept on the GPU after the first evaluation of the fit (MG_OPT_FIT_RESIDENT 0)"),
+                   "resident_target": bool(a.resident)},
         "published": {"plain_s": PUBLISHED_S["plain"], "ti_s": PUBLISHED_S["ti"],
                       "hardware": "LRZ CoolMUC-4 node, 112 OpenMP threads",
                       "source": "benchmark_hpc/bench_out/q16/plots/n5_q16_u601_invariance_scaling.txt:10-11"},

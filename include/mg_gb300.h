@@ -61,11 +61,16 @@ int mg_get_precision(void);
  * brickwall Hessian) is computed.  0 (default): one forward-mode sweep per basis column,
  * block and entry, which adds each of the block's gates' placeholder terms as it passes them
  * (a sixth of the gate steps at L=16 with 5 layers); 1: one sweep per gate and entry, the
- * reference's placements (src/matchgate_brickwall.c:177-231).  The two agree to rounding. */
+ * reference's placements (src/matchgate_brickwall.c:177-231).  The two agree to rounding.
+ * FIT_RESIDENT: 0 (default) lets mg_optimize_brickwall / mg_optimize_circuit keep a GPU
+ * circuit target's columns on the GPU for the duration of the fit (the target is fixed
+ * there) when they take at most a quarter of the free device memory (2^(2L-1) x 16 bytes:
+ * 32 GiB at L=16), so only the first evaluation sweeps the target; 1 sweeps it in every
+ * evaluation, as the reference applies its target map each time.  Results are the same. */
 enum { MG_OPT_TILE_BITS = 1, MG_OPT_THREADS = 2, MG_OPT_CHUNK_COLUMNS = 3, MG_OPT_CTAS_PER_SM = 4,
        MG_OPT_TARGET_TILE_BITS = 5, MG_OPT_TARGET_THREADS = 6, MG_OPT_TARGET_COLUMNS = 7,
        MG_OPT_TRANSLATIONAL_INVARIANCE = 8, MG_OPT_TARGET_DENSE = 9, MG_OPT_HOST_THREADS = 10,
-       MG_OPT_FIT_CACHE = 11, MG_OPT_TARGET_TUNE = 12, MG_OPT_HESS_GROUP = 13 };
+       MG_OPT_FIT_CACHE = 11, MG_OPT_TARGET_TUNE = 12, MG_OPT_HESS_GROUP = 13, MG_OPT_FIT_RESIDENT = 14 };
 int mg_set_option(int option, long value);
 long mg_get_option(int option);
 

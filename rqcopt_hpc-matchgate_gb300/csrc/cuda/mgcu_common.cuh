@@ -47,6 +47,12 @@ struct DevBuf
 		n = bytes;
 		return 0;
 	}
+	void release()
+	{
+		if (p) cudaFree(p);
+		p = nullptr;
+		n = 0;
+	}
 	template <class T> T* as() const { return reinterpret_cast<T*>(p); }
 };
 

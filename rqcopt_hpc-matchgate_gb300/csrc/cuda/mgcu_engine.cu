@@ -2311,8 +2311,15 @@ extern "C" void mgcu_target_set_resident(mgcu_target* t, int enable)
 {
 	t->resident = enable;
 	if (!enable)
-		for (int i = 0; i < 3; i++) { t->res_valid[i] = false; }
+		for (int i = 0; i < 3; i++)
+		{
+			t->res_valid[i] = false;
+			t->res_cols[i].release();
+		}
 }
+// 1 when the target keeps its columns resident, 0 when not, -1 for a dense target (whose
+// columns are never swept)
+extern "C" int mgcu_target_resident(const mgcu_target* t) { return t->kind == 0 ? t->resident : -1; }
 
 extern "C" int mgcu_target_apply(mgcu_target* t, const mgc* psi, mgc* out)
 {

@@ -89,6 +89,12 @@ extern "C" void mgcu_stream_destroy(void* s)
 void mgcu_count_launch(long n) { g_launches += n; }
 
 extern "C" long mgcu_launch_count(void) { return g_launches.load(); }
+extern "C" double mgcu_device_free_bytes(void)
+{
+	size_t f = 0, t = 0;
+	if (!mgcu_ctx() || cudaMemGetInfo(&f, &t) != cudaSuccess) return 0;
+	return (double)f;
+}
 
 // ------------------------------------------------------------------------------------
 // Peak arithmetic rates: every thread runs 8 independent FMA chains; the chains'

@@ -115,6 +115,16 @@ int mg_target_set_resident(void* udata, int enable)
 	return 0;
 }
 
+int mgh_target_resident(void* udata)
+{
+	mg_target_handle* h = (mg_target_handle*)udata;
+	if (!h || h->magic != MG_TARGET_MAGIC) return -1;
+	mgcu_lock();
+	const int r = mgcu_target_resident(h->dev);
+	mgcu_unlock();
+	return r;
+}
+
 int mg_target_conserves_weight(void* udata)
 {
 	mg_target_handle* h = (mg_target_handle*)udata;

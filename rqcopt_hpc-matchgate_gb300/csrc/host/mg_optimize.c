@@ -12,6 +12,12 @@
  * general circuit with one parameter block per gate.  The last f_iter entry, f at the final
  * iterate, reuses the evaluation of the accepted trial point that became that iterate (the
  * reference evaluates the same point once more; the value is the same, bit for bit).
+ *
+ * The target does not change during a fit, so (MG_OPT_FIT_RESIDENT 0, the default) its
+ * conjugated columns stay on the GPU after the first evaluation when they take at most a
+ * quarter of the free device memory, and every later evaluation skips the target sweep; the
+ * columns are the same the sweep would produce (same program, same bits), and they are
+ * released when the fit ends unless the caller had made the target resident itself.
  */
 #include <complex.h>
 #include <math.h>
@@ -97,6 +103,12 @@ static int optimize(void* target, const struct matchgate vlist0[], const fit_t* 
 	memcpy(x, vlist0, sizeof(struct matchgate) * nlayers);
 	plans_t pl = { 0 };
 	int prec = refine_gnorm > 0 ? MG_PREC_MIXED : MG_PREC_FP64;
+	int made_resident = 0;
+	if (mgcu_option(MG_OPT_FIT_RESIDENT_ID) != 1 && mgh_target_resident(target) == 0)
+	{
+		const double bytes = ldexp(1.0, 2 * fit->L - 1) * 16.0;   /* float-float and complex128 columns */
+		if (bytes <= 0.25 * mgcu_device_free_bytes() && mg_target_set_resident(target, 1) == 0) made_resident = 1;
+	}
 	int rc = plans_make(&pl, target, x, fit, prec);
 	double radius = params->radius_init;
 	/* f of the current iterate from a target-only evaluation at the current precision, when
@@ -156,6 +168,7 @@ static int optimize(void* target, const struct matchgate vlist0[], const fit_t* 
 		memcpy(vlist_out, x, sizeof(struct matchgate) * nlayers);
 	}
 	plans_free(&pl);
+	if (made_resident) mg_target_set_resident(target, 0);
 	free(x); free(xn); free(grad); free(H); free(eta);
 	return rc;
 }

@@ -39,7 +39,8 @@ extern "C" {
 #define MG_OPT_FIT_CACHE_ID     11
 #define MG_OPT_TARGET_TUNE_ID   12
 #define MG_OPT_HESS_GROUP_ID    13
-#define MG_NOPTIONS             13
+#define MG_OPT_FIT_RESIDENT_ID  14
+#define MG_NOPTIONS             14
 
 /* ---- runtime ---- */
 /* streams: each host thread issues its GPU work on its own stream when it selected one
@@ -80,6 +81,10 @@ void mgcu_target_destroy(mgcu_target* t);
 int mgcu_target_apply(mgcu_target* t, const mgc* psi, mgc* out);      /* host vectors */
 int mgcu_target_L(const mgcu_target* t);
 void mgcu_target_set_resident(mgcu_target* t, int enable);
+int mgcu_target_resident(const mgcu_target* t);
+double mgcu_device_free_bytes(void);
+/* host layer: residency of a GPU target handle (-1: not a GPU circuit target) */
+int mgh_target_resident(void* udata);
 int mgcu_target_sweep_gates(mgcu_target* t);
 int mgcu_target_conserves_weight(mgcu_target* t);
 

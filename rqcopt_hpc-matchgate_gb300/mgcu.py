@@ -29,6 +29,7 @@ OPT_HOST_THREADS = 10
 OPT_FIT_CACHE = 11
 OPT_TARGET_TUNE = 12
 OPT_HESS_GROUP = 13
+OPT_FIT_RESIDENT = 14
 EVAL_TARGET, EVAL_GRADIENT, EVAL_HESSIAN, EVAL_TI = 0, 1, 2, 4
 
 P = C.c_void_p
