@@ -154,3 +154,26 @@ def test_native_trust_region_and_refinement(lib, oracle):
     assert np.max(np.abs(f64 - f_o)) < 1e-8 and udist(v64, v_o) < 1e-8
     assert pmx[0] == mgcu.PREC_MIXED and pmx[-1] == mgcu.PREC_FP64
     assert np.max(np.abs(fmx - f_o)) < 1e-9 * np.max(np.abs(f_o)) and udist(vmx, v_o) < 1e-8
+
+
+def test_native_fit_resident_columns_are_bit_identical(lib):
+    """mg_optimize_brickwall keeps the target's columns on the GPU during the fit
+    (MG_OPT_FIT_RESIDENT 0); sweeping the target in every evaluation instead (1) gives the
+    same iterates bit for bit, in complex128 and with the float-float to complex128 switch"""
+    rng = np.random.default_rng(3)
+    L, nl, ul = 10, 3, 6
+    perms = brickwall_perms(L, nl)
+    uperms = brickwall_perms(L, ul)
+    t = lib.target_brickwall(random_gates(ul, rng, unitary=True), uperms, L)
+    v0 = random_gates(nl, rng, unitary=True)
+    out = []
+    try:
+        for res in (0, 1):
+            lib.set_option(mgcu.OPT_FIT_RESIDENT, res)
+            out.append((lib.optimize_native(t, v0, perms, L, 6), lib.optimize_native(t, v0, perms, L, 6, refine_gnorm=5.0)))
+    finally:
+        lib.set_option(mgcu.OPT_FIT_RESIDENT, 0)
+        lib.set_precision(mgcu.PREC_FP64)
+        lib.target_free(t)
+    for a, b in zip(out[0], out[1]):
+        assert np.array_equal(a[0], b[0]) and np.array_equal(a[1], b[1]) and np.array_equal(a[2], b[2])
