@@ -468,13 +468,16 @@ def run_secondary(a):
     if a.config == "hess14" and a.profile_hessian:
         lib.set_precision(mgcu.PREC_MIXED)
         lib.set_option(mgcu.OPT_CHUNK_COLUMNS, a.profile_hessian)
-        cg = np.array([v[l] for l in range(nl) for _ in range(L // 2)])
-        cw = np.array([[perms[l][2 * i], perms[l][2 * i + 1]] for l in range(nl) for i in range(L // 2)], np.int32)
-        rc, f, dg, H = lib.circuit_target_gradient_hessian(lib.mg_target_apply, target, cg, cw, L)
+        if a.hessian == "layer":   # the per-layer Hessian: grouped items, one per layer and entry
+            rc, f, dg, H = lib.brickwall_target_gradient_hessian(lib.mg_target_apply, target, v, perms, L)
+        else:
+            cg = np.array([v[l] for l in range(nl) for _ in range(L // 2)])
+            cw = np.array([[perms[l][2 * i], perms[l][2 * i + 1]] for l in range(nl) for i in range(L // 2)], np.int32)
+            rc, f, dg, H = lib.circuit_target_gradient_hessian(lib.mg_target_apply, target, cg, cw, L)
         assert rc == 0, lib.last_error()
         lib.set_option(mgcu.OPT_CHUNK_COLUMNS, 0)
         lib.target_free(target)
-        print(json.dumps({"profile_hessian": a.profile_hessian, "L": L, "f": [f.real, f.imag]}))
+        print(json.dumps({"profile_hessian": a.profile_hessian, "hessian": a.hessian, "L": L, "f": [f.real, f.imag]}))
         return
     res = {}
     for name, prec in (("mixed", mgcu.PREC_MIXED), ("fp64", mgcu.PREC_FP64)):
