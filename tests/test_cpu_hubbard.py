@@ -106,3 +106,35 @@ def test_spinless_brickwall_matches_python_construction(mglib, L, nsteps, order)
 def test_spinless_brickwall_bad_arguments(mglib):
     for args in [(5, 1.0, 1.5, 1.0, 2, 2), (16, 1.0, 1.5, 1.0, 0, 2), (16, 1.0, 1.5, 1.0, 2, 3)]:
         assert mglib.lib.mg_spinless_hubbard_brickwall(*args, None, None, 0) < 0
+
+
+@pytest.mark.parametrize("order", [2, 4, 6])
+def test_spinless_brickwall_orders_approach_exact_evolution(mglib, order):
+    """the spinless brickwall's layers are exp(-i tau h) on every bond of the ring, h =
+    -J (|01><10| + |10><01|) + g |11><11| (the two-qubit operator the layers exponentiate, the
+    periodic bond included as is); its error against exp(-i H t), H the sum of h over all
+    bonds, falls as h^order when the steps double"""
+    L, J, g, t = 6, 1.0, 1.5, 0.6
+    h = np.zeros((4, 4), complex)
+    h[1, 2] = h[2, 1] = -J
+    h[3, 3] = g
+    n = 1 << L
+    H = np.zeros((n, n), complex)
+    for i in range(L):
+        j = (i + 1) % L
+        for a in range(n):
+            bi, bj = (a >> (L - 1 - i)) & 1, (a >> (L - 1 - j)) & 1
+            for oi in (0, 1):
+                for oj in (0, 1):
+                    v = h[2 * oi + oj, 2 * bi + bj]
+                    if v != 0:
+                        b2 = a & ~(1 << (L - 1 - i)) & ~(1 << (L - 1 - j)) | (oi << (L - 1 - i)) | (oj << (L - 1 - j))
+                        H[b2, a] += v
+    Uex = scipy.linalg.expm(-1j * t * H)
+    e = []
+    for nsteps in (2, 4):
+        u, pm = mglib.spinless_hubbard_brickwall(L, J, g, t, nsteps, order)
+        gates = np.array([u[l] for l in range(len(u)) for _ in range(L // 2)])
+        wires = np.array([[pm[l][2 * p], pm[l][2 * p + 1]] for l in range(len(u)) for p in range(L // 2)], np.int32)
+        e.append(np.linalg.norm(T.circuit_unitary(gates, wires, L) - Uex, 2))
+    assert 0.6 * 2 ** order < e[0] / e[1] < 1.5 * 2 ** order, (order, e)
